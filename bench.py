@@ -1,0 +1,378 @@
+#!/usr/bin/env python
+"""Benchmark: FFT-based 3D convolutions per second on GB300 (one JSON line on rank 0).
+
+Workload (the size the headline metric is quoted on): 4 convolutions of 256^3 complex64
+signals (re/im i.i.d. N(0,1)) with per-signal complex64 filters (re/im U[-1,1]), seeded
+synthetic data. One step = one batch of 4 convolutions through the library's C ABI.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--path fp32|tc]
+
+value      : convolutions/s with inputs resident in HBM (convgpu_conv3d_device), all ranks.
+e2e        : convolutions/s through convgpu_conv3d_host with pinned host buffers; every step
+             copies its inputs host->device and its outputs device->host.
+roofline   : the dominant pass kernel: algorithmic bytes per launch / mean launch time, timed
+             with CUDA events on its stream during the timed region, against the measured HBM
+             copy bandwidth of MEASURED_PEAKS.json.
+cpu_baseline: the CPU FFT convolution (pocketfft complex64, all host threads; FFTW3 is not
+             installed) on a bounded sample, rank 0 at N=1 only.
+--impl reference: times that CPU implementation alone as the reference arm.
+
+Multi-GPU (torchrun, one rank per GPU): every rank convolves its own batch of 4 (independent
+convolutions, no collective on the data path); value = all ranks' convolutions / max time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "3D FFT-conv/s + HBM GB/s at 256^3 c64: TC split vs plain FP32, rel-L2≤1e-5"
+N, BATCH = 256, 4
+WORKLOAD = "256^3 complex64 x4 convolutions, per-signal filters"
+
+
+def _args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=200)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--path", choices=["fp32", "tc"], default="fp32")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    a = p.parse_args()
+    a.warmup = max(a.warmup, 3)
+    return a
+
+
+def _dist():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def _config(path: str) -> dict:
+    return {
+        "workload": WORKLOAD,
+        "n": N,
+        "batch": BATCH,
+        "filters": "per-signal",
+        "path": {"fp32": "plain FP32 per-axis passes", "tc": "tensor-core BF16x3 split"}[path],
+        "normalised": False,
+        "l2": "no flush: each step reads 1 GiB of inputs (> 129 MB L2)",
+    }
+
+
+# --------------------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_bench_{device}.csv")
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "100",
+                 "-i", str(self.device)], stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict | None:
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.fh.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    mx.append(float(parts[2]))
+                except ValueError:
+                    continue
+                for nm, v in zip(names, parts[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+# --------------------------------------------------------------------------- CPU side
+def _cpu_conv_sample(frac: float, sig, filt, workers: int) -> float:
+    """Seconds for `frac` of one FFT convolution (filter FFT, signal FFT, multiply,
+    inverse FFT) with pocketfft complex64 — the reference CPU path's operations
+    (src/fft_conv3D.cpp:137-160) on a slab of planes / columns."""
+    import numpy as np
+    import scipy.fft as sfft
+
+    from oracle import comp_mult
+
+    n = sig.shape[-1]
+    m = max(1, int(round(frac * n)))
+    t0 = time.perf_counter()
+    if m >= n:
+        fs = sfft.fftn(filt, workers=workers)
+        ss = sfft.fftn(sig, workers=workers)
+        prod = comp_mult(ss, fs)
+        sfft.ifftn(prod, norm="forward", workers=workers)
+    else:
+        for a in (filt, sig):  # same operation count as the full transforms, on m/n of the lines
+            b = sfft.fftn(a[:m], axes=(1, 2), workers=workers)
+            sfft.fft(a[:, :m, :], axis=0, workers=workers)
+        prod = comp_mult(b, b)
+        sfft.fftn(prod, axes=(1, 2), workers=workers)
+        sfft.fft(sig[:, :m, :], axis=0, workers=workers)
+    return time.perf_counter() - t0
+
+
+def _cpu_inputs():
+    import numpy as np
+
+    rng = np.random.default_rng(3)
+    sig = np.empty((N, N, N), np.complex64)
+    sig.real = rng.standard_normal((N, N, N), dtype=np.float32)
+    sig.imag = rng.standard_normal((N, N, N), dtype=np.float32)
+    filt = np.empty((N, N, N), np.complex64)
+    filt.real = rng.uniform(-1, 1, (N, N, N)).astype(np.float32)
+    filt.imag = rng.uniform(-1, 1, (N, N, N)).astype(np.float32)
+    return sig, filt
+
+
+def cpu_baseline(budget_s: float = 20.0) -> dict:
+    workers = os.cpu_count() or 1
+    sig, filt = _cpu_inputs()
+    _cpu_conv_sample(0.25, sig, filt, workers)  # warm-up (plans, page faults)
+    t1 = _cpu_conv_sample(1.0, sig, filt, workers)
+    reps = max(2, min(5, int(budget_s / max(t1, 1e-3))))
+    ts = [t1] + [_cpu_conv_sample(1.0, sig, filt, workers) for _ in range(reps - 1)]
+    med = statistics.median(ts)
+    return {"value": 1.0 / med, "unit": "conv/s", "cores": workers, "kind": "port",
+            "sample": f"median of {len(ts)} single 256^3 convolutions (filter FFT + signal FFT + multiply + "
+                      f"inverse FFT, pocketfft complex64, {workers} threads; FFTW3 unavailable - pocketfft "
+                      f"stand-in), one of the 4 per step"}
+
+
+def run_reference(a) -> None:
+    rank, world, _ = _dist()
+    if rank != 0:
+        return
+    workers = os.cpu_count() or 1
+    sig, filt = _cpu_inputs()
+    _cpu_conv_sample(0.25, sig, filt, workers)
+    t1 = _cpu_conv_sample(1.0, sig, filt, workers)
+    # Each step is one convolution, or a fixed fraction of one when K+W full convolutions
+    # would take longer than about three minutes.
+    frac = min(1.0, 170.0 / ((a.steps + a.warmup) * t1))
+    m = max(1, int(round(frac * N)))
+    frac = m / N
+    for _ in range(a.warmup):
+        _cpu_conv_sample(frac, sig, filt, workers)
+    tot = 0.0
+    for _ in range(a.steps):
+        tot += _cpu_conv_sample(frac, sig, filt, workers)
+    conv_s = a.steps * frac / tot
+    sample = (f"each step: {'one' if frac >= 1 else f'{m}/{N} of one'} 256^3 convolution with its own filter "
+              f"(filter FFT + signal FFT + multiply + inverse FFT), pocketfft complex64, {workers} threads "
+              f"(FFTW3 unavailable - pocketfft stand-in for src/fft_conv3D.cpp:50-177)")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": conv_s, "unit": "conv/s", "n_gpus": world,
+        "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 * tot / a.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": _config("fp32"),
+        "cpu_baseline": {"value": conv_s, "unit": "conv/s", "cores": workers, "kind": "port", "sample": sample},
+        "e2e": {"value": conv_s, "unit": "conv/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# --------------------------------------------------------------------------- GPU side
+def run_ours(a) -> None:
+    import torch
+
+    import convfpga_gb300 as cg
+
+    rank, world, local = _dist()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    if not os.path.exists(cg.LIB_PATH):
+        from convfpga_gb300 import build
+
+        build.build()
+    rc = cg.fpga_initialize(f"cuda:{local}", "convgpu_plans.json", False)
+    if rc != 0:
+        raise SystemExit(f"fpga_initialize failed: {rc} {cg.last_error()}")
+
+    flags = cg.FILTER_PER_SIGNAL | (cg.TENSOR_SPLIT if a.path == "tc" else 0)
+    g = torch.Generator(device="cuda").manual_seed(1234 + rank)
+    shape = (BATCH, N, N, N)
+    sig = torch.complex(torch.randn(shape, device="cuda", generator=g),
+                        torch.randn(shape, device="cuda", generator=g))
+    filt = torch.complex(torch.rand(shape, device="cuda", generator=g) * 2 - 1,
+                         torch.rand(shape, device="cuda", generator=g) * 2 - 1)
+    out = torch.empty_like(sig)
+    stream = torch.cuda.current_stream()
+
+    def step():
+        cg.conv3d_device(N, sig, filt, out, BATCH, flags, stream)
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+
+    for _ in range(a.warmup):
+        step()
+    torch.cuda.synchronize()
+    barrier()
+    torch.cuda.synchronize()
+
+    sampler = ClockSampler(local)
+    sampler.start()
+    launches0 = cg.launch_count()
+    cg.pass_timing_start()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(a.steps):
+        step()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    gpu_launches = cg.launch_count() - launches0
+    passes = cg.pass_timing_read()
+    cg.pass_timing_stop()
+    ms = ev0.elapsed_time(ev1)
+    if world > 1:
+        import torch.distributed as dist
+
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_step = ms / a.steps
+    value = world * BATCH * a.steps / (ms / 1e3)
+
+    peak, peak_kind = _peaks()
+    dom_name, dom = max(passes.items(), key=lambda kv: kv[1]["ms"])
+    per_launch_bytes = dom["bytes"] / dom["launches"]
+    per_launch_s = dom["ms"] / dom["launches"] / 1e3
+    achieved = per_launch_bytes / per_launch_s / 1e9
+    traffic = _read_traffic(dom_name)
+    model_bytes = BATCH * 136 * N ** 3  # per step: 48 N^3 per filter + 88 N^3 per signal
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": traffic, "kernel": dom_name,
+                "bytes_per_launch": per_launch_bytes, "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"
+                if peak_kind == "measured" else "fallback 6.8 TB/s",
+                "share_of_step": round(dom["ms"] / sum(p["ms"] for p in passes.values()), 3)}
+
+    # e2e through the host-buffer C ABI entry point with pinned buffers.
+    vol = BATCH * N ** 3
+    hs = cg.PinnedBuffer.alloc(vol * 8)
+    hf = cg.PinnedBuffer.alloc(vol * 8)
+    ho = cg.PinnedBuffer.alloc(vol * 8)
+    sig_h, filt_h, out_h = hs.array(shape), hf.array(shape), ho.array(shape)
+    sig_h[...] = sig.cpu().numpy()
+    filt_h[...] = filt.cpu().numpy()
+    e2e_flags = cg.FILTER_PER_SIGNAL
+    for _ in range(2):
+        t = cg.conv3d_host(N, hs.ptr, hf.ptr, ho.ptr, BATCH, e2e_flags)
+        assert t.valid, cg.last_error()
+    e2e_steps = max(3, min(a.steps, 20))
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        t = cg.conv3d_host(N, hs.ptr, hf.ptr, ho.ptr, BATCH, e2e_flags)
+    e2e_s = time.perf_counter() - t0
+    assert t.valid, cg.last_error()
+    if world > 1:
+        import torch.distributed as dist
+
+        tt = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e_s = float(tt.item())
+    e2e = {"value": world * BATCH * e2e_steps / e2e_s, "unit": "conv/s",
+           "h2d_bytes_per_step": 2 * vol * 8, "d2h_bytes_per_step": vol * 8,
+           "api": "convgpu_conv3d_host (pinned host buffers)",
+           "last_call_ms": {k: round(v, 3) for k, v in t.as_dict().items() if k != "valid"}}
+    for b in (hs, hf, ho):
+        b.free()
+
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": "conv/s", "n_gpus": world, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "bf16x3" if a.path == "tc" else "f32",
+        "data": "synthetic (seeded torch generator; signals N(0,1), filters U[-1,1])",
+        "config": _config(a.path),
+        "hbm_gbs_model": round(model_bytes / (ms_step / 1e3) / 1e9, 1),
+        "roofline": roofline,
+        "passes": {k: {"ms_per_launch": round(v["ms"] / v["launches"], 4), "launches": v["launches"],
+                       "gbs": round(v["bytes"] / (v["ms"] / 1e3) / 1e9, 1)} for k, v in passes.items()},
+        "e2e": e2e,
+        "gpu_launches": gpu_launches,
+        "clocks": clocks,
+    }
+    if world == 1 and not a.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline()
+    print(json.dumps(line), flush=True)
+
+
+def _read_traffic(kernel: str):
+    """DRAM bytes per launch of the dominant kernel from the committed ncu summary, if any."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "dram_traffic.json")) as f:
+            d = json.load(f)
+        return d.get(kernel)
+    except Exception:
+        return None
+
+
+def main():
+    a = _args()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_ours(a)
+
+
+if __name__ == "__main__":
+    main()

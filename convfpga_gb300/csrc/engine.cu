@@ -1,0 +1,603 @@
+// Runtime of the GB300 FFT convolution library: device selection, streams, workspace,
+// the pass sequence of one convolution, and the pipelined host-buffer path.
+//
+// Reference behaviour mirrored here (host/src/*.c of pc2/ConvFPGA):
+//  - fpga_initialize return codes 0 / -1..-5 (host/src/fpga_init.c:48-56, 57-121);
+//  - conv entry points return fpga_t{valid=0} on NULL pointers or a non-power-of-two N
+//    (host/src/convfpga.c:36-37) and never exit() on runtime errors (the reference's
+//    checkError does: host/src/opencl_utils.c:421-439);
+//  - outputs are unnormalised (x N^3) unless the caller asks for 1/N^3;
+//  - fpga_t times in milliseconds, taken from device events like the reference's
+//    OpenCL event profiling (host/src/convfpga.c:83-85, 169-172, 276-279, 360-375).
+//
+// Pass sequence of one convolution (per signal, 5 HBM passes; the reference streams
+// 3 phases with a DDR transpose inside each 3D FFT, host/src/convfpga.c:74-363):
+//   filter (shared):      x-fwd -> y-fwd -> z-fwd              (filter spectrum in workspace)
+//   filter (per signal):  x-fwd -> y-fwd                       (z done inside CONV_FZ)
+//   signal:               x-fwd -> y-fwd -> z[fwd, (.)F, inv] -> y-inv -> x-inv(scale)
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "abi_bridge.h"
+#include "engine_internal.h"
+#include "passes.cuh"
+
+namespace convgpu {
+
+// Flag bits shared with include/convgpu.h.
+constexpr unsigned kFlagNormalize = 1u << 0;
+constexpr unsigned kFlagPerSignalFilter = 1u << 1;
+constexpr unsigned kFlagFilterIsSpectrum = 1u << 2;
+constexpr unsigned kFlagTensorSplit = 1u << 3;
+
+constexpr int kErrInval = -1;
+constexpr int kErrNotInit = -2;
+constexpr int kErrCuda = -3;
+constexpr int kErrNoMem = -4;
+constexpr int kErrUnsupported = -5;
+
+static thread_local std::string g_err;
+static std::atomic<unsigned long long> g_launches{0};
+
+void count_launches(unsigned long long k) { g_launches.fetch_add(k, std::memory_order_relaxed); }
+
+static void set_err(const std::string &s) { g_err = s; }
+static int cuda_fail(cudaError_t e, const char *what) {
+  set_err(std::string(what) + ": " + cudaGetErrorString(e));
+  return (e == cudaErrorMemoryAllocation) ? kErrNoMem : kErrCuda;
+}
+
+static bool valid_n(unsigned n) { return n >= 16 && n <= 512 && (n & (n - 1)) == 0; }
+
+// Grow-only device buffer. Growing synchronises the device first, so work still in
+// flight on the old block never sees it freed.
+struct DevBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+  cudaError_t ensure(size_t b) {
+    if (b <= bytes) return cudaSuccess;
+    if (p) {
+      cudaDeviceSynchronize();
+      cudaFree(p);
+      p = nullptr;
+      bytes = 0;
+    }
+    cudaError_t e = cudaMalloc(&p, b);
+    if (e == cudaSuccess) bytes = b;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+};
+
+struct Engine {
+  std::recursive_mutex mu;
+  bool init = false;
+  int device = 0;
+  bool use_svm = false;
+  int pageable_access = 0;
+  int sm_count = 0;
+  cudaStream_t sc = nullptr, sh2d = nullptr, sd2h = nullptr;
+  float2 *tw512 = nullptr;
+  DevBuf ws;           // device API workspace (filter spectra)
+  DevBuf hfilt;        // host API: filter input / spectrum
+  DevBuf hio[3];       // host API: signal chunk buffers
+  DevBuf hfio[3];      // host API: per-signal filter chunk buffers
+  std::string plan_path;
+};
+static Engine g;
+
+static cudaError_t upload_twiddles(float2 **dst) {
+  std::vector<float2> h(512);
+  const double two_pi = 6.283185307179586476925286766559;
+  for (int j = 0; j < 512; ++j) {
+    const double a = -two_pi * (double)j / 512.0;
+    h[j] = make_float2((float)std::cos(a), (float)std::sin(a));
+  }
+  cudaError_t e = cudaMalloc(dst, 512 * sizeof(float2));
+  if (e != cudaSuccess) return e;
+  return cudaMemcpy(*dst, h.data(), 512 * sizeof(float2), cudaMemcpyHostToDevice);
+}
+
+static void teardown_locked() {
+  if (!g.init) return;
+  cudaSetDevice(g.device);
+  cudaDeviceSynchronize();
+  g.ws.release();
+  g.hfilt.release();
+  for (auto &b : g.hio) b.release();
+  for (auto &b : g.hfio) b.release();
+  if (g.tw512) cudaFree(g.tw512);
+  g.tw512 = nullptr;
+  if (g.sc) cudaStreamDestroy(g.sc);
+  if (g.sh2d) cudaStreamDestroy(g.sh2d);
+  if (g.sd2h) cudaStreamDestroy(g.sd2h);
+  g.sc = g.sh2d = g.sd2h = nullptr;
+  g.init = false;
+}
+
+// Sets up the runtime on `dev`. Returns 0 or a negative fpga_initialize-style code.
+static int setup_locked(int dev, bool use_svm) {
+  if (g.init && g.device == dev) {
+    g.use_svm = g.use_svm || use_svm;
+    return 0;
+  }
+  teardown_locked();
+  cudaError_t e = cudaSetDevice(dev);
+  if (e != cudaSuccess) {
+    set_err(std::string("cudaSetDevice: ") + cudaGetErrorString(e));
+    return -3;
+  }
+  cudaDeviceGetAttribute(&g.pageable_access, cudaDevAttrPageableMemoryAccess, dev);
+  cudaDeviceGetAttribute(&g.sm_count, cudaDevAttrMultiProcessorCount, dev);
+  int can_map = 0;
+  cudaDeviceGetAttribute(&can_map, cudaDevAttrCanMapHostMemory, dev);
+  if (use_svm && !can_map && !g.pageable_access) {
+    set_err("device cannot address host memory");
+    return -5;
+  }
+  // The kernels are built for sm_103a only; a device they cannot load on is the
+  // analogue of a bitstream that fails to load (-4).
+  e = probe_kernel_image();
+  if (e != cudaSuccess) {
+    set_err(std::string("kernel image not loadable on this device: ") + cudaGetErrorString(e));
+    cudaGetLastError();
+    return -4;
+  }
+  if ((e = cudaStreamCreateWithFlags(&g.sc, cudaStreamNonBlocking)) != cudaSuccess ||
+      (e = cudaStreamCreateWithFlags(&g.sh2d, cudaStreamNonBlocking)) != cudaSuccess ||
+      (e = cudaStreamCreateWithFlags(&g.sd2h, cudaStreamNonBlocking)) != cudaSuccess ||
+      (e = upload_twiddles(&g.tw512)) != cudaSuccess) {
+    set_err(std::string("runtime setup: ") + cudaGetErrorString(e));
+    g.init = true;  // let teardown release what was created
+    teardown_locked();
+    return -4;
+  }
+  g.device = dev;
+  g.use_svm = use_svm;
+  g.init = true;
+  return 0;
+}
+
+// Lazily initialises on the caller's current device (device / extension entry points).
+static int ensure_init_locked() {
+  if (g.init) return cudaSetDevice(g.device) == cudaSuccess ? 0 : kErrCuda;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    set_err("no CUDA device");
+    return kErrNotInit;
+  }
+  return setup_locked(dev, false) == 0 ? 0 : kErrNotInit;
+}
+
+// ------------------------------------------------------------------ pass timing
+// Optional per-pass timing: events around every pass on its own stream, summed per
+// (axis, op) slot with the pass's algorithmic bytes (one read + one write of every
+// cube, plus one read of the filter operand for the fused z pass).
+constexpr int kSlots = 12;  // slot = axis * 4 + op
+struct PassRec {
+  int slot;
+  double bytes;
+  cudaEvent_t a, b;
+};
+static bool g_prof = false;
+static std::vector<PassRec> g_prof_recs;
+
+static cudaError_t pass(int n, int axis, int op, const float2 *src, float2 *dst, const float2 *filt,
+                        long long filt_vol, int nvol, float scale, cudaStream_t s) {
+  PassRec r{axis * 4 + op, 0.0, nullptr, nullptr};
+  if (g_prof) {
+    const double vol = (double)n * n * n * 8.0 * nvol;
+    r.bytes = 2.0 * vol + ((op == OP_CONV || op == OP_CONV_FZ) ? vol : 0.0);
+    cudaEventCreate(&r.a);
+    cudaEventCreate(&r.b);
+    cudaEventRecord(r.a, s);
+  }
+  cudaError_t e = launch_axis_pass(n, axis, op, src, dst, filt, filt_vol, nvol, scale, g.tw512, s);
+  if (g_prof) {
+    cudaEventRecord(r.b, s);
+    g_prof_recs.push_back(r);
+  }
+  return e;
+}
+
+// ------------------------------------------------------------------ pass sequences
+#define CG_TRY(expr)                        \
+  do {                                      \
+    cudaError_t _e = (expr);                \
+    if (_e != cudaSuccess) return _e;       \
+    count_launches(1);                      \
+  } while (0)
+
+// Filter spectra of `count` filters (x, y and, unless xy_only, z passes) into spec.
+static cudaError_t enqueue_filter(int n, const float2 *filt, float2 *spec, int count, bool xy_only,
+                                  cudaStream_t s) {
+  CG_TRY(pass(n, 0, OP_FWD, filt, spec, nullptr, 0, count, 1.f, s));
+  CG_TRY(pass(n, 1, OP_FWD, spec, spec, nullptr, 0, count, 1.f, s));
+  if (!xy_only) CG_TRY(pass(n, 2, OP_FWD, spec, spec, nullptr, 0, count, 1.f, s));
+  return cudaSuccess;
+}
+
+// Signal passes. fop: OP_CONV (spec is a full spectrum) or OP_CONV_FZ (xy only).
+// mid (optional) is recorded after the fused z pass.
+static cudaError_t enqueue_signals(int n, const float2 *sig, float2 *out, const float2 *spec,
+                                   long long spec_vol, int fop, int nsig, float scale, cudaStream_t s,
+                                   cudaEvent_t mid) {
+  CG_TRY(pass(n, 0, OP_FWD, sig, out, nullptr, 0, nsig, 1.f, s));
+  CG_TRY(pass(n, 1, OP_FWD, out, out, nullptr, 0, nsig, 1.f, s));
+  CG_TRY(pass(n, 2, fop, out, out, spec, spec_vol, nsig, 1.f, s));
+  if (mid) cudaEventRecord(mid, s);
+  CG_TRY(pass(n, 1, OP_INV, out, out, nullptr, 0, nsig, 1.f, s));
+  CG_TRY(pass(n, 0, OP_INV, out, out, nullptr, 0, nsig, scale, s));
+  return cudaSuccess;
+}
+
+static size_t workspace_bytes_for(unsigned n, unsigned how_many, unsigned flags) {
+  const size_t vol = (size_t)n * n * n * sizeof(float2);
+  if (flags & kFlagFilterIsSpectrum) return 0;
+  if (flags & kFlagPerSignalFilter) return vol * how_many;
+  return vol;
+}
+
+// Whole convolution on device pointers, enqueued on stream s using workspace ws.
+static cudaError_t enqueue_conv_device(unsigned n, const float2 *sig, const float2 *filt, float2 *out,
+                                       unsigned how_many, unsigned flags, float2 *ws, cudaStream_t s) {
+  const float scale = (flags & kFlagNormalize) ? (float)(1.0 / ((double)n * n * n)) : 1.0f;
+  const long long V = (long long)n * n * n;
+  if (flags & kFlagFilterIsSpectrum) {
+    const long long sv = (flags & kFlagPerSignalFilter) ? V : 0;
+    return enqueue_signals(n, sig, out, filt, sv, OP_CONV, how_many, scale, s, nullptr);
+  }
+  if (flags & kFlagPerSignalFilter) {
+    cudaError_t e = enqueue_filter(n, filt, ws, how_many, true, s);
+    if (e != cudaSuccess) return e;
+    return enqueue_signals(n, sig, out, ws, V, OP_CONV_FZ, how_many, scale, s, nullptr);
+  }
+  cudaError_t e = enqueue_filter(n, filt, ws, 1, false, s);
+  if (e != cudaSuccess) return e;
+  return enqueue_signals(n, sig, out, ws, 0, OP_CONV, how_many, scale, s, nullptr);
+}
+
+// ------------------------------------------------------------------ bridge: setup
+int bridge_initialize(const char *platform_name, const char *path, bool use_svm) {
+  std::lock_guard<std::recursive_mutex> lk(g.mu);
+  if (path == nullptr || path[0] == '\0') {
+    set_err("path missing");
+    return -1;
+  }
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+    cudaGetLastError();
+    set_err("no CUDA devices");
+    return -3;
+  }
+  int dev = 0;
+  // "cuda:K" / "gpu:K" selects device K; any other name (the reference app passes the
+  // Intel FPGA platform names) means the first device, as fpga_initialize picks
+  // devices[0] (host/src/fpga_init.c:86).
+  if (platform_name) {
+    const char *p = nullptr;
+    if (std::strncmp(platform_name, "cuda:", 5) == 0) p = platform_name + 5;
+    if (std::strncmp(platform_name, "gpu:", 4) == 0) p = platform_name + 4;
+    if (p) {
+      char *end = nullptr;
+      long k = std::strtol(p, &end, 10);
+      if (end == p || *end != '\0' || k < 0 || k >= count) {
+        set_err("no such CUDA device");
+        return -2;
+      }
+      dev = (int)k;
+    }
+  }
+  g.plan_path = path;
+  return setup_locked(dev, use_svm);
+}
+
+void bridge_final() {
+  std::lock_guard<std::recursive_mutex> lk(g.mu);
+  teardown_locked();
+}
+
+// ------------------------------------------------------------------ bridge: device API
+int bridge_workspace_bytes(unsigned n, unsigned how_many, unsigned flags, size_t *bytes) {
+  if (!bytes || !valid_n(n) || how_many == 0) return kErrInval;
+  *bytes = workspace_bytes_for(n, how_many, flags);
+  return 0;
+}
+
+int bridge_conv_device(unsigned n, const void *d_sig, const void *d_filt, void *d_out, unsigned how_many,
+                       unsigned flags, void *stream) {
+  if (!d_sig || !d_filt || !d_out || !valid_n(n)) {
+    set_err("invalid arguments");
+    return kErrInval;
+  }
+  if (how_many == 0) return 0;
+  if (flags & kFlagTensorSplit) {
+    set_err("tensor-core split path not available in this build");
+    return kErrUnsupported;
+  }
+  std::lock_guard<std::recursive_mutex> lk(g.mu);
+  int rc = ensure_init_locked();
+  if (rc) return rc;
+  cudaError_t e = g.ws.ensure(workspace_bytes_for(n, how_many, flags));
+  if (e != cudaSuccess) return cuda_fail(e, "workspace");
+  e = enqueue_conv_device(n, (const float2 *)d_sig, (const float2 *)d_filt, (float2 *)d_out, how_many, flags,
+                          (float2 *)g.ws.p, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(e, "launch");
+  return 0;
+}
+
+int bridge_filter_spectrum_device(unsigned n, const void *d_filt, void *d_spec, unsigned count, void *stream) {
+  if (!d_filt || !d_spec || !valid_n(n)) {
+    set_err("invalid arguments");
+    return kErrInval;
+  }
+  if (count == 0) return 0;
+  std::lock_guard<std::recursive_mutex> lk(g.mu);
+  int rc = ensure_init_locked();
+  if (rc) return rc;
+  cudaError_t e = enqueue_filter(n, (const float2 *)d_filt, (float2 *)d_spec, count, false, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(e, "launch");
+  return 0;
+}
+
+int bridge_conv_uneven_device(const UnevenJob *jobs, unsigned njobs, const void *d_sig, const void *d_filt,
+                              void *d_out, unsigned flags, void *stream) {
+  if (!jobs || !d_sig || !d_filt || !d_out) {
+    set_err("invalid arguments");
+    return kErrInval;
+  }
+  for (unsigned j = 0; j < njobs; ++j)
+    if (!valid_n(jobs[j].n)) {
+      set_err("job with unsupported size");
+      return kErrInval;
+    }
+  std::lock_guard<std::recursive_mutex> lk(g.mu);
+  int rc = ensure_init_locked();
+  if (rc) return rc;
+  // One job at a time; the persistent work-queue launch replaces this loop.
+  size_t need = 0;
+  for (unsigned j = 0; j < njobs; ++j) need = std::max(need, workspace_bytes_for(jobs[j].n, 1, flags & ~kFlagPerSignalFilter));
+  cudaError_t e = g.ws.ensure(need);
+  if (e != cudaSuccess) return cuda_fail(e, "workspace");
+  for (unsigned j = 0; j < njobs; ++j) {
+    const float2 *s = (const float2 *)d_sig + jobs[j].sig_off;
+    const float2 *f = (const float2 *)d_filt + jobs[j].filt_off;
+    float2 *o = (float2 *)d_out + jobs[j].out_off;
+    e = enqueue_conv_device(jobs[j].n, s, f, o, 1, flags & ~kFlagPerSignalFilter, (float2 *)g.ws.p,
+                            (cudaStream_t)stream);
+    if (e != cudaSuccess) return cuda_fail(e, "launch");
+  }
+  return 0;
+}
+
+// ------------------------------------------------------------------ bridge: host API
+namespace {
+struct EvPool {
+  std::vector<cudaEvent_t> ev;
+  cudaEvent_t get() {
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    ev.push_back(e);
+    return e;
+  }
+  ~EvPool() {
+    for (auto e : ev) cudaEventDestroy(e);
+  }
+};
+float ms_between(cudaEvent_t a, cudaEvent_t b) {
+  float ms = 0.f;
+  if (cudaEventElapsedTime(&ms, a, b) != cudaSuccess) return 0.f;
+  return ms;
+}
+}  // namespace
+
+Timing bridge_conv_host(unsigned n, const void *sig, const void *filt, void *out, unsigned how_many,
+                        unsigned flags, int mode) {
+  Timing t{0, 0, 0, 0, 0, 0, false};
+  if (sig == nullptr || filt == nullptr || out == nullptr || !valid_n(n)) {
+    set_err("invalid arguments");
+    return t;
+  }
+  if (how_many == 0) {
+    set_err("how_many is 0");
+    return t;
+  }
+  if (flags & (kFlagTensorSplit | kFlagFilterIsSpectrum)) {
+    set_err("flag not supported by the host-buffer entry points");
+    return t;
+  }
+  std::lock_guard<std::recursive_mutex> lk(g.mu);
+  if (ensure_init_locked() != 0) return t;
+  (void)mode;
+
+  const bool per_signal = (flags & kFlagPerSignalFilter) != 0;
+  const size_t V = (size_t)n * n * n;
+  const size_t vbytes = V * sizeof(float2);
+  const float scale = (flags & kFlagNormalize) ? (float)(1.0 / ((double)V)) : 1.0f;
+  // Signals per chunk: at least one cube, about 64 MiB per chunk otherwise.
+  const unsigned per_chunk = (unsigned)std::max<size_t>(1, std::min<size_t>(how_many, (64u << 20) / vbytes));
+  const unsigned nchunks = (how_many + per_chunk - 1) / per_chunk;
+  const unsigned nbuf = std::min(3u, nchunks);
+
+  cudaError_t e = cudaSuccess;
+  for (unsigned b = 0; b < nbuf && e == cudaSuccess; ++b) {
+    e = g.hio[b].ensure(per_chunk * vbytes);
+    if (e == cudaSuccess && per_signal) e = g.hfio[b].ensure(per_chunk * vbytes);
+  }
+  if (e == cudaSuccess) e = g.hfilt.ensure(vbytes * (per_signal ? per_chunk : 1));
+  if (e != cudaSuccess) {
+    cuda_fail(e, "device buffers");
+    return t;
+  }
+
+  EvPool pool;
+  cudaEvent_t f0 = pool.get(), f1 = pool.get(), f2 = pool.get();
+  std::vector<cudaEvent_t> h0(nchunks), h1(nchunks), c0(nchunks), c1(nchunks), cm(nchunks), d0(nchunks),
+      d1(nchunks), freed(nbuf);
+  for (unsigned c = 0; c < nchunks; ++c) {
+    h0[c] = pool.get();
+    h1[c] = pool.get();
+    c0[c] = pool.get();
+    c1[c] = pool.get();
+    cm[c] = pool.get();
+    d0[c] = pool.get();
+    d1[c] = pool.get();
+  }
+  for (unsigned b = 0; b < nbuf; ++b) freed[b] = pool.get();
+
+  float2 *fspec = (float2 *)g.hfilt.p;
+  if (!per_signal) {
+    cudaEventRecord(f0, g.sh2d);
+    e = cudaMemcpyAsync(fspec, filt, vbytes, cudaMemcpyHostToDevice, g.sh2d);
+    cudaEventRecord(f1, g.sh2d);
+    cudaStreamWaitEvent(g.sc, f1, 0);
+    if (e == cudaSuccess) e = enqueue_filter(n, fspec, fspec, 1, false, g.sc);
+    cudaEventRecord(f2, g.sc);
+  }
+
+  for (unsigned c = 0; c < nchunks && e == cudaSuccess; ++c) {
+    const unsigned b = c % nbuf;
+    const unsigned first = c * per_chunk;
+    const unsigned cnt = std::min(per_chunk, how_many - first);
+    float2 *io = (float2 *)g.hio[b].p;
+    if (c >= nbuf) cudaStreamWaitEvent(g.sh2d, freed[b], 0);
+    cudaEventRecord(h0[c], g.sh2d);
+    e = cudaMemcpyAsync(io, (const float2 *)sig + (size_t)first * V, cnt * vbytes, cudaMemcpyHostToDevice, g.sh2d);
+    if (e == cudaSuccess && per_signal)
+      e = cudaMemcpyAsync(g.hfio[b].p, (const float2 *)filt + (size_t)first * V, cnt * vbytes,
+                          cudaMemcpyHostToDevice, g.sh2d);
+    cudaEventRecord(h1[c], g.sh2d);
+    if (e != cudaSuccess) break;
+    cudaStreamWaitEvent(g.sc, h1[c], 0);
+    cudaEventRecord(c0[c], g.sc);
+    if (per_signal) {
+      e = enqueue_filter(n, (const float2 *)g.hfio[b].p, (float2 *)g.hfio[b].p, cnt, true, g.sc);
+      if (e == cudaSuccess)
+        e = enqueue_signals(n, io, io, (const float2 *)g.hfio[b].p, (long long)V, OP_CONV_FZ, cnt, scale, g.sc,
+                            cm[c]);
+    } else {
+      e = enqueue_signals(n, io, io, fspec, 0, OP_CONV, cnt, scale, g.sc, cm[c]);
+    }
+    cudaEventRecord(c1[c], g.sc);
+    if (e != cudaSuccess) break;
+    cudaStreamWaitEvent(g.sd2h, c1[c], 0);
+    cudaEventRecord(d0[c], g.sd2h);
+    e = cudaMemcpyAsync((float2 *)out + (size_t)first * V, io, cnt * vbytes, cudaMemcpyDeviceToHost, g.sd2h);
+    cudaEventRecord(d1[c], g.sd2h);
+    cudaEventRecord(freed[b], g.sd2h);
+  }
+  cudaError_t es = cudaStreamSynchronize(g.sd2h);
+  cudaError_t es2 = cudaStreamSynchronize(g.sc);
+  cudaError_t es3 = cudaStreamSynchronize(g.sh2d);
+  if (e == cudaSuccess) e = es != cudaSuccess ? es : (es2 != cudaSuccess ? es2 : es3);
+  if (e != cudaSuccess) {
+    cuda_fail(e, "host pipeline");
+    return t;
+  }
+  if (!per_signal) {
+    t.filter_pcie_wr_t = ms_between(f0, f1);
+    t.filter_exec_t = ms_between(f1, f2);
+  }
+  double inv = 0.0;
+  for (unsigned c = 0; c < nchunks; ++c) {
+    t.sig_pcie_wr_t += ms_between(h0[c], h1[c]);
+    t.sig_exec_t += ms_between(c0[c], cm[c]);
+    inv += ms_between(cm[c], c1[c]);
+    t.sig_pcie_rd_t += ms_between(d0[c], d1[c]);
+  }
+  // Single call: forward phase vs inverse phase. Batched call: like the reference,
+  // sig_exec_t sums the per-signal compute phases and siginv_exec_t is the wall span
+  // from the first compute to the last (host/src/convfpga_svm_batch.c:664-665).
+  if (mode == HOST_BATCH) {
+    t.sig_exec_t += inv;
+    t.siginv_exec_t = ms_between(c0[0], c1[nchunks - 1]);
+  } else {
+    t.siginv_exec_t = inv;
+  }
+  t.valid = true;
+  return t;
+}
+
+// ------------------------------------------------------------------ bridge: misc
+int bridge_device_info(int *device, int *pageable_access, int *sm_count) {
+  std::lock_guard<std::recursive_mutex> lk(g.mu);
+  int rc = ensure_init_locked();
+  if (rc) return rc;
+  if (device) *device = g.device;
+  if (pageable_access) *pageable_access = g.pageable_access;
+  if (sm_count) *sm_count = g.sm_count;
+  return 0;
+}
+
+unsigned long long bridge_launch_count() { return g_launches.load(); }
+
+int bridge_pass_timing(int mode, double *ms, unsigned long long *launches, double *bytes) {
+  std::lock_guard<std::recursive_mutex> lk(g.mu);
+  auto clear = [] {
+    for (auto &r : g_prof_recs) {
+      cudaEventDestroy(r.a);
+      cudaEventDestroy(r.b);
+    }
+    g_prof_recs.clear();
+  };
+  if (mode == 0 || mode == 1) {
+    if (g.init) cudaDeviceSynchronize();
+    clear();
+    g_prof = (mode == 1);
+    return 0;
+  }
+  if (mode != 2 || !ms || !launches || !bytes) return kErrInval;
+  for (int i = 0; i < kSlots; ++i) {
+    ms[i] = 0.0;
+    launches[i] = 0;
+    bytes[i] = 0.0;
+  }
+  for (auto &r : g_prof_recs) {
+    cudaEventSynchronize(r.b);
+    float t = 0.f;
+    if (cudaEventElapsedTime(&t, r.a, r.b) != cudaSuccess) return cuda_fail(cudaGetLastError(), "pass timing");
+    ms[r.slot] += t;
+    launches[r.slot] += 1;
+    bytes[r.slot] += r.bytes;
+  }
+  return 0;
+}
+
+const char *bridge_last_error() { return g_err.c_str(); }
+
+int bridge_host_alloc_pinned(size_t bytes, void **ptr) {
+  if (!ptr) return kErrInval;
+  *ptr = nullptr;
+  if (bytes == 0) return 0;
+  cudaError_t e = cudaHostAlloc(ptr, bytes, cudaHostAllocPortable);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaHostAlloc");
+  return 0;
+}
+
+int bridge_host_free_pinned(void *ptr) {
+  if (!ptr) return 0;
+  cudaError_t e = cudaFreeHost(ptr);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaFreeHost");
+  return 0;
+}
+
+int bridge_sync() {
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) return cuda_fail(e, "synchronize");
+  return 0;
+}
+
+}  // namespace convgpu

@@ -1,0 +1,25 @@
+// Internal interface between the CUDA translation units (kernels + runtime).
+// Uses CUDA's float2; never include the public convfpga.h next to this header
+// (that header declares its own `float2`).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+
+namespace convgpu {
+
+// Launches one per-axis pass over `nvol` cubes of size n (axis 0 = x, 1 = y, 2 = z).
+// op: OP_FWD / OP_INV / OP_CONV / OP_CONV_FZ (passes.cuh). src may equal dst.
+cudaError_t launch_axis_pass(int n, int axis, int op, const float2 *src, float2 *dst, const float2 *filt,
+                             long long filt_vol_elems, int nvol, float scale, const float2 *tw512,
+                             cudaStream_t s);
+
+// Checks that this library's kernel image loads on the current device.
+cudaError_t probe_kernel_image();
+
+// Counts kernel launches issued by this library (host-side, monotonic).
+void count_launches(unsigned long long k);
+
+}  // namespace convgpu

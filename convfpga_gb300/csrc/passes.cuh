@@ -1,0 +1,166 @@
+// Per-axis FFT pass kernels for complex64 cubes (x fastest: idx = z*N*N + y*N + x).
+//
+// One launch transforms every pencil of one axis of a batch of cubes in place (or from
+// src to dst). The reference builds each 3D transform from three streaming 1D engines
+// joined by an on-chip plane transpose and a DDR round-trip transpose
+// (kernels/conv3D.cl:71-420: fft3da, transpose, fft3db, transpose3D, fft3dc, store).
+// Here each axis is one pass over HBM:
+//   - x pass: pencils are contiguous rows; a CTA owns COLS consecutive rows.
+//   - y / z passes: pencils are strided (N or N*N elements); a CTA owns COLS adjacent
+//     x-columns of one plane, so every global access is a run of COLS*8 contiguous bytes.
+// The transposes disappear: strided pencils are gathered straight into registers.
+//
+// Fused ops (Op):
+//   FWD      forward transform.
+//   INV      unnormalised backward transform, results multiplied by `scale`.
+//   CONV     forward z transform, pointwise product with a filter spectrum read at the
+//            same positions (conv3D / comp_mult: kernels/conv3D.cl:517-570,
+//            kernels/fft/fft_8.cl:180-185), backward z transform. The spectrum never
+//            leaves registers.
+//   CONV_FZ  as CONV, but the filter operand is only x/y transformed: its z transform
+//            is computed in the same kernel (per-signal filters: saves one filter pass).
+#pragma once
+
+#include <cstdint>
+
+#include "fft_core.cuh"
+
+namespace convgpu {
+
+enum PassOp : int { OP_FWD = 0, OP_INV = 1, OP_CONV = 2, OP_CONV_FZ = 3 };
+
+struct PassArgs {
+  const float2 *src;
+  float2 *dst;
+  const float2 *filt;      // CONV / CONV_FZ only
+  const float2 *tw512;     // tw512[j] = exp(-2*pi*i*j/512), j < 512 (FP64-generated)
+  long long vol_elems;     // N^3
+  long long filt_vol_elems;  // 0: one filter for all volumes; N^3: one per volume
+  long long axis_stride;   // elements between consecutive pencil positions (strided passes)
+  long long plane_pitch;   // strided: element offset per group row (N*N for y, N for z)
+  int groups_per_vol;      // CTAs per volume
+  int groups_x;            // strided: N / COLS
+  float scale;             // INV / CONV: output scale
+};
+
+// Shared-memory slot of pencil position n for the two layouts.
+template <int COLS>
+struct ColSlot {  // strided passes: position-major, columns contiguous (conflict-free)
+  int c;
+  __device__ __forceinline__ int operator()(int n) const { return n * COLS + c; }
+};
+template <int N>
+struct RowSlot {  // x pass: pencil-major, one 8-byte pad every 16 slots
+  int base;
+  __device__ __forceinline__ int operator()(int n) const { return base + n + (n >> 4); }
+};
+template <int N>
+constexpr int row_pitch() { return N + N / 16; }
+
+template <int N, int E, int NS, class SIdx, int R, int... Rest>
+__device__ __forceinline__ void run_stages(float2 (&v)[E], int t, const float2 *tw, float2 *sm, const SIdx &sidx) {
+  constexpr int T = N / E;
+  constexpr bool last = sizeof...(Rest) == 0;
+  stockham_stage<N, E, R, NS, last>(v, t, tw, sm, sidx);
+  if constexpr (!last) {
+    __syncthreads();
+#pragma unroll
+    for (int e = 0; e < E; ++e) v[e] = sm[sidx(t + e * T)];
+    __syncthreads();
+    run_stages<N, E, NS * R, SIdx, Rest...>(v, t, tw, sm, sidx);
+  }
+}
+
+template <int N, int E, class SIdx, int... Rs>
+__device__ __forceinline__ void fft_forward(float2 (&v)[E], int t, const float2 *tw, float2 *sm, const SIdx &sidx,
+                                            Radices<Rs...>) {
+  (void)PlanCheck<N, E, Radices<Rs...>>::stages;
+  run_stages<N, E, 1, SIdx, Rs...>(v, t, tw, sm, sidx);
+}
+
+template <int E>
+__device__ __forceinline__ void swap_all(float2 (&v)[E]) {
+#pragma unroll
+  for (int e = 0; e < E; ++e) v[e] = cswap(v[e]);
+}
+
+// Dynamic shared memory: N twiddles, then the exchange buffer.
+template <int N, int E, int COLS, bool CONTIG>
+constexpr int pass_smem_bytes() {
+  return (N + (CONTIG ? COLS * row_pitch<N>() : COLS * N)) * 8;
+}
+
+template <int N, int E, int COLS, bool CONTIG, int OP, class Plan>
+__global__ void __launch_bounds__(COLS *(N / E)) k_axis_pass(PassArgs a) {
+  constexpr int T = N / E;
+  extern __shared__ float2 smem[];
+  float2 *tw = smem;
+  float2 *sm = smem + N;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = a.tw512[i * (512 / N)];
+
+  int t, c;
+  long long base, fbase, es;
+  if constexpr (CONTIG) {
+    t = threadIdx.x % T;
+    c = threadIdx.x / T;
+    const long long row = (long long)blockIdx.x * COLS + c;
+    base = row * N;
+    const long long vol = row / ((long long)N * N);
+    fbase = vol * a.filt_vol_elems + (row % ((long long)N * N)) * N;
+    es = 1;
+  } else {
+    c = threadIdx.x % COLS;
+    t = threadIdx.x / COLS;
+    const long long vol = blockIdx.x / a.groups_per_vol;
+    const int r = blockIdx.x % a.groups_per_vol;
+    const long long outer = (long long)(r / a.groups_x) * a.plane_pitch + (long long)(r % a.groups_x) * COLS + c;
+    base = vol * a.vol_elems + outer;
+    fbase = vol * a.filt_vol_elems + outer;
+    es = a.axis_stride;
+  }
+  auto sidx = [&]() {
+    if constexpr (CONTIG) return RowSlot<N>{c * row_pitch<N>()};
+    else return ColSlot<COLS>{c};
+  }();
+
+  float2 v[E];
+#pragma unroll
+  for (int e = 0; e < E; ++e) v[e] = a.src[base + (long long)(t + e * T) * es];
+  __syncthreads();  // twiddle table ready
+
+  if constexpr (OP == OP_FWD) {
+    fft_forward<N, E>(v, t, tw, sm, sidx, Plan{});
+  } else if constexpr (OP == OP_INV) {
+    swap_all(v);
+    fft_forward<N, E>(v, t, tw, sm, sidx, Plan{});
+    swap_all(v);
+    if (a.scale != 1.0f) {
+#pragma unroll
+      for (int e = 0; e < E; ++e) v[e] = make_float2(v[e].x * a.scale, v[e].y * a.scale);
+    }
+  } else {
+    float2 f[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) f[e] = a.filt[fbase + (long long)(t + e * T) * es];
+    if constexpr (OP == OP_CONV_FZ) {
+      fft_forward<N, E>(f, t, tw, sm, sidx, Plan{});
+      __syncthreads();
+    }
+    fft_forward<N, E>(v, t, tw, sm, sidx, Plan{});
+#pragma unroll
+    for (int e = 0; e < E; ++e) v[e] = cmul(v[e], f[e]);
+    __syncthreads();
+    swap_all(v);
+    fft_forward<N, E>(v, t, tw, sm, sidx, Plan{});
+    swap_all(v);
+    if (a.scale != 1.0f) {
+#pragma unroll
+      for (int e = 0; e < E; ++e) v[e] = make_float2(v[e].x * a.scale, v[e].y * a.scale);
+    }
+  }
+
+#pragma unroll
+  for (int e = 0; e < E; ++e) a.dst[base + (long long)(t + e * T) * es] = v[e];
+}
+
+}  // namespace convgpu

@@ -1,0 +1,107 @@
+/*
+ * convgpu.h — extensions of the GB300 FFT convolution library beyond convfpga.h.
+ *
+ * None of these has a counterpart in pc2/ConvFPGA; each extends one of its entry
+ * points, named below. Device-pointer entry points are stream-ordered: they enqueue
+ * work on `stream` (a cudaStream_t passed as void*, NULL = legacy default stream)
+ * and return without waiting. They return 0 on success or a negative CONVGPU_E*
+ * code; convgpu_last_error() describes the last failure of the calling thread.
+ *
+ * Data layout everywhere: complex64 (float2) cubes of N^3 points, x fastest
+ * (idx = z*N*N + y*N + x), cube i of a batch at offset i*N^3.
+ */
+#ifndef CONVGPU_H
+#define CONVGPU_H
+
+#include "convfpga.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Flags */
+#define CONVGPU_NORMALIZE (1u << 0)            /* scale outputs by 1/N^3 */
+#define CONVGPU_FILTER_PER_SIGNAL (1u << 1)    /* filter holds how_many cubes, one per signal */
+#define CONVGPU_FILTER_IS_SPECTRUM (1u << 2)   /* filter already holds FFT3(filter) */
+#define CONVGPU_TENSOR_SPLIT (1u << 3)         /* tensor-core split-precision path */
+
+/* Status codes */
+#define CONVGPU_OK 0
+#define CONVGPU_EINVAL (-1)
+#define CONVGPU_ENOTINIT (-2)
+#define CONVGPU_ECUDA (-3)
+#define CONVGPU_ENOMEM (-4)
+#define CONVGPU_EUNSUPPORTED (-5)
+
+/* how_many convolutions on DEVICE pointers, enqueued on `stream`.
+ * Extends fpgaf_conv3D_svm_batch (host/include/convfpga/convfpga.h:46) with device
+ * buffers, per-signal filters (CONVGPU_FILTER_PER_SIGNAL), precomputed spectra
+ * (CONVGPU_FILTER_IS_SPECTRUM), normalisation and the tensor-core path.
+ * d_sig may equal d_out (in place). The library's per-device workspace is shared by
+ * all calls: calls on different streams must not overlap. */
+int convgpu_conv3d_device(unsigned N, const float2 *d_sig, const float2 *d_filter, float2 *d_out,
+                          unsigned how_many, unsigned flags, void *stream);
+
+/* Host-buffer batch with the flags above (CONVGPU_TENSOR_SPLIT and
+ * CONVGPU_FILTER_IS_SPECTRUM excluded). Copies overlap compute on separate streams;
+ * pinned buffers (convgpu_host_alloc) copy fastest.
+ * Extends fpgaf_conv3D_svm_batch (host/include/convfpga/convfpga.h:46). */
+fpga_t convgpu_conv3d_host(unsigned N, const float2 *sig, const float2 *filter, float2 *out,
+                           unsigned how_many, unsigned flags);
+
+/* FFT3 of `count` filter cubes into d_spectrum (count*N^3 float2), for reuse with
+ * CONVGPU_FILTER_IS_SPECTRUM: the reference transforms the filter on every call
+ * (host/src/convfpga.c:74-172). */
+int convgpu_filter_spectrum_device(unsigned N, const float2 *d_filter, float2 *d_spectrum, unsigned count,
+                                   void *stream);
+
+/* One entry of an uneven batch: cube size and element offsets from the base pointers. */
+typedef struct {
+  unsigned n;
+  unsigned long long sig_offset;
+  unsigned long long filter_offset;
+  unsigned long long out_offset;
+} convgpu_job;
+
+/* Convolutions of different power-of-two sizes in one call (one filter per job),
+ * on device pointers. Extends fpgaf_conv3D_svm_batch to uneven sizes. */
+int convgpu_conv3d_uneven_device(const convgpu_job *jobs, unsigned njobs, const float2 *d_sig_base,
+                                 const float2 *d_filter_base, float2 *d_out_base, unsigned flags, void *stream);
+
+/* Bytes of device workspace convgpu_conv3d_device uses for these arguments. */
+int convgpu_workspace_bytes(unsigned N, unsigned how_many, unsigned flags, size_t *bytes);
+
+/* Pinned (page-locked) host memory for fast copies; release with convgpu_host_free. */
+int convgpu_host_alloc(size_t bytes, void **ptr);
+int convgpu_host_free(void *ptr);
+
+/* Device in use, whether it can read pageable host memory, and its SM count. */
+int convgpu_device_info(int *device, int *pageable_access, int *sm_count);
+
+/* Number of kernels this library has launched so far in the process. */
+unsigned long long convgpu_launch_count(void);
+
+/* Per-pass device timing, the analogue of the reference's per-phase OpenCL event
+ * profiling (host/src/convfpga.c:83-85, 169-172, 276-279, 360-363).
+ *   mode 1: clear and start recording (events around every pass on its stream)
+ *   mode 0: clear and stop
+ *   mode 2: wait for the recorded passes and fill the CONVGPU_PASS_SLOTS arrays:
+ *           ms[slot] total milliseconds, launches[slot] count, bytes[slot] algorithmic
+ *           bytes (one read + one write of every cube, plus the filter operand read of
+ *           the fused z pass); slot = axis * 4 + op, axis 0/1/2 = x/y/z,
+ *           op 0 forward, 1 inverse, 2 z fwd->multiply->inv, 3 same with the filter's
+ *           z transform fused in. */
+#define CONVGPU_PASS_SLOTS 12
+int convgpu_pass_timing(int mode, double *ms, unsigned long long *launches, double *bytes);
+
+/* Waits for all work on the library's device. */
+int convgpu_synchronize(void);
+
+/* Text of the calling thread's last error ("" if none). */
+const char *convgpu_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CONVGPU_H */

@@ -1,0 +1,193 @@
+"""GPU parity of the plain FP32 path, through the C ABI, against the oracle.
+
+Criterion: the reference's own, SNR > 120 dB (relative L2 < 1e-6) against the FP32
+pipeline of src/fft_conv3D.cpp:186-258 (src/fft_conv3D.cpp:236-258), and against the
+golden vectors of the reference's FFT engine. Full-size workloads are also checked
+against the FP64 oracle and through size-independent properties.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import conv3d, gaussian_filter, make_config, max_abs, rel_l2, snr_db
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+SNR_DB = 120.0
+
+
+def _c64(rng, shape):
+    a = np.empty(shape, np.complex64)
+    a.real = rng.uniform(-1, 1, shape)
+    a.imag = rng.uniform(-1, 1, shape)
+    return a
+
+
+def dev_conv(cg, sig, filt, flags=0, inplace=False):
+    n = sig.shape[-1]
+    b = sig.shape[0]
+    s = torch.from_numpy(np.ascontiguousarray(sig)).cuda()
+    f = torch.from_numpy(np.ascontiguousarray(filt)).cuda()
+    o = s if inplace else torch.empty_like(s)
+    cg.conv3d_device(n, s, f, o, b, flags)
+    torch.cuda.synchronize()
+    return o.cpu().numpy()
+
+
+@pytest.mark.parametrize("name", ["conv16x3", "conv16x2pf", "conv32x1"])
+def test_golden_reference_engine(gpu, name):
+    d = np.load(os.path.join(GOLD, f"{name}.npz"))
+    flags = gpu.FILTER_PER_SIGNAL if d["filt"].ndim == 4 else 0
+    out = dev_conv(gpu, d["sig"], d["filt"], flags)
+    assert snr_db(d["out"], out) > SNR_DB
+
+
+def test_golden_64_workload(gpu):
+    d = np.load(os.path.join(GOLD, "conv64x1.npz"))
+    sig, filt, _ = make_config("c64x1")
+    out = dev_conv(gpu, sig, filt)
+    assert snr_db(d["out"], out) > SNR_DB
+
+
+@pytest.mark.parametrize("n", [16, 32, 64, 128, 256])
+@pytest.mark.parametrize("per_signal", [False, True])
+def test_sizes_against_fp32_oracle(gpu, n, per_signal):
+    rng = np.random.default_rng(n + 7 * per_signal)
+    b = 2 if n <= 128 else 1
+    sig = _c64(rng, (b, n, n, n))
+    filt = _c64(rng, (b, n, n, n)) if per_signal else _c64(rng, (n, n, n))
+    out = dev_conv(gpu, sig, filt, gpu.FILTER_PER_SIGNAL if per_signal else 0)
+    ref = conv3d(sig, filt, "fp32", engine="pocketfft")
+    assert snr_db(ref, out) > SNR_DB
+    ref64 = conv3d(sig, filt, "fp64", engine="pocketfft")
+    assert rel_l2(ref64, out) < 1e-6
+
+
+@pytest.mark.slow
+def test_512_against_fp32_oracle(gpu):
+    rng = np.random.default_rng(512)
+    n = 512
+    sig = _c64(rng, (1, n, n, n))
+    filt = gaussian_filter(n, 6.0)
+    out = dev_conv(gpu, sig, filt)
+    ref = conv3d(sig, filt, "fp32", engine="pocketfft")
+    assert snr_db(ref, out) > SNR_DB
+
+
+def test_normalise_and_inplace(gpu):
+    rng = np.random.default_rng(3)
+    n = 64
+    sig = _c64(rng, (3, n, n, n))
+    filt = _c64(rng, (n, n, n))
+    ref = conv3d(sig, filt, "fp32", normalize=True, engine="pocketfft")
+    out = dev_conv(gpu, sig, filt, gpu.NORMALIZE, inplace=True)
+    assert snr_db(ref, out) > SNR_DB
+
+
+def test_filter_spectrum_reuse(gpu):
+    rng = np.random.default_rng(4)
+    n = 32
+    sig = _c64(rng, (2, n, n, n))
+    filt = _c64(rng, (n, n, n))
+    f = torch.from_numpy(filt).cuda()
+    spec = torch.empty_like(f)
+    gpu.filter_spectrum_device(n, f, spec, 1)
+    torch.cuda.synchronize()
+    spec_ref = np.fft.fftn(filt.astype(np.complex128))
+    assert rel_l2(spec_ref, spec.cpu().numpy()) < 1e-6
+    out = dev_conv(gpu, sig, spec.cpu().numpy(), gpu.FILTER_IS_SPECTRUM)
+    assert snr_db(conv3d(sig, filt, "fp32", engine="pocketfft"), out) > SNR_DB
+
+
+@pytest.mark.parametrize("fn", ["fpgaf_conv3D", "fpgaf_conv3D_svm"])
+def test_reference_host_entry_points(gpu, fn):
+    rng = np.random.default_rng(5)
+    n = 64
+    sig = _c64(rng, (n, n, n))
+    filt = _c64(rng, (n, n, n))
+    out = np.zeros_like(sig)
+    t = getattr(gpu, fn)(n, sig, filt, out)
+    assert t.valid, gpu.last_error()
+    assert t.filter_exec_t > 0 and t.sig_exec_t > 0 and t.sig_pcie_wr_t > 0 and t.sig_pcie_rd_t > 0
+    assert snr_db(conv3d(sig, filt, "fp32", engine="pocketfft"), out) > SNR_DB
+
+
+@pytest.mark.parametrize("how_many", [1, 3, 4])
+def test_batch_entry_point_any_count_distinct_signals(gpu, how_many):
+    """Odd counts and distinct signals per slot (the reference breaks on both:
+    host/src/convfpga_svm_batch.c:302, 579-648; src/helper.cpp:159-171)."""
+    rng = np.random.default_rng(6 + how_many)
+    n = 32
+    sig = _c64(rng, (how_many, n, n, n))
+    filt = _c64(rng, (n, n, n))
+    out = np.zeros_like(sig)
+    t = gpu.fpgaf_conv3D_svm_batch(n, sig, filt, out, how_many)
+    assert t.valid, gpu.last_error()
+    ref = conv3d(sig, filt, "fp32", engine="pocketfft")
+    for i in range(how_many):
+        assert snr_db(ref[i], out[i]) > SNR_DB
+
+
+def test_host_batch_chunked_per_signal(gpu):
+    """More signals than one 64 MiB chunk: exercises the 3-buffer copy/compute pipeline."""
+    rng = np.random.default_rng(8)
+    n, b = 128, 7
+    sig = _c64(rng, (b, n, n, n))
+    filt = _c64(rng, (b, n, n, n))
+    out = np.zeros_like(sig)
+    t = gpu.conv3d_host(n, sig, filt, out, b, gpu.FILTER_PER_SIGNAL | gpu.NORMALIZE)
+    assert t.valid, gpu.last_error()
+    ref = conv3d(sig, filt, "fp32", normalize=True, engine="pocketfft")
+    assert snr_db(ref, out) > SNR_DB
+
+
+def test_uneven_jobs(gpu):
+    rng = np.random.default_rng(9)
+    sizes = [32, 64, 16, 128, 32]
+    sigs = [_c64(rng, (n, n, n)) for n in sizes]
+    filts = [gaussian_filter(n, 2.0 + i) for i, n in enumerate(sizes)]
+    offs = np.cumsum([0] + [n ** 3 for n in sizes])
+    s = torch.from_numpy(np.concatenate([x.ravel() for x in sigs])).cuda()
+    f = torch.from_numpy(np.concatenate([x.ravel() for x in filts])).cuda()
+    o = torch.empty_like(s)
+    jobs = [(n, int(offs[i]), int(offs[i]), int(offs[i])) for i, n in enumerate(sizes)]
+    gpu.conv3d_uneven_device(jobs, s, f, o, gpu.NORMALIZE)
+    torch.cuda.synchronize()
+    oh = o.cpu().numpy()
+    for i, n in enumerate(sizes):
+        ref = conv3d(sigs[i], filts[i], "fp32", normalize=True, engine="pocketfft")
+        got = oh[offs[i]:offs[i + 1]].reshape(n, n, n)
+        assert snr_db(ref, got) > SNR_DB
+
+
+@pytest.mark.slow
+def test_full_size_256x4_against_fp64(gpu):
+    sig, filt, _ = make_config("c256x4")
+    out = dev_conv(gpu, sig, filt, gpu.FILTER_PER_SIGNAL | gpu.NORMALIZE)
+    ref = conv3d(sig[:1], filt[:1], "fp64", normalize=True, engine="pocketfft")
+    assert rel_l2(ref, out[:1]) < 1e-6
+    assert max_abs(ref, out[:1]) < 1e-5 * np.abs(ref).max()
+
+
+@pytest.mark.slow
+@pytest.mark.parametrize("n", [256, 512])
+def test_full_size_properties(gpu, n):
+    """Size-independent checks at the full cube sizes: a shifted delta filter is a
+    circular shift (exact up to rounding), and the operator is linear."""
+    rng = np.random.default_rng(n)
+    sig = np.empty((1, n, n, n), np.complex64)
+    sig.real = rng.standard_normal((1, n, n, n), dtype=np.float32)
+    sig.imag = rng.standard_normal((1, n, n, n), dtype=np.float32)
+    delta = np.zeros((n, n, n), np.complex64)
+    delta[3, 5, 7] = 1.0
+    out = dev_conv(gpu, sig, delta, gpu.NORMALIZE)
+    shifted = np.roll(sig, shift=(3, 5, 7), axis=(1, 2, 3))
+    assert rel_l2(shifted, out) < 1e-6
+    if n == 256:
+        g = gaussian_filter(n, 4.0)
+        a = dev_conv(gpu, sig, g, gpu.NORMALIZE)
+        b = dev_conv(gpu, 2.0 * sig, g, gpu.NORMALIZE)
+        assert rel_l2(2.0 * a, b) < 1e-6
