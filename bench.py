@@ -46,6 +46,8 @@ def _args():
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--path", choices=["fp32", "tc"], default="fp32")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling runs)")
+    p.add_argument("--batch", type=int, default=BATCH, help="cubes per step (profiling runs use 1)")
     a = p.parse_args()
     a.warmup = max(a.warmup, 3)
     return a
@@ -238,6 +240,8 @@ def run_ours(a) -> None:
     if rc != 0:
         raise SystemExit(f"fpga_initialize failed: {rc} {cg.last_error()}")
 
+    global BATCH
+    BATCH = a.batch
     flags = cg.FILTER_PER_SIGNAL | (cg.TENSOR_SPLIT if a.path == "tc" else 0)
     g = torch.Generator(device="cuda").manual_seed(1234 + rank)
     shape = (BATCH, N, N, N)
@@ -304,6 +308,32 @@ def run_ours(a) -> None:
                 "share_of_step": round(dom["ms"] / sum(p["ms"] for p in passes.values()), 3)}
 
     # e2e through the host-buffer C ABI entry point with pinned buffers.
+    e2e = _e2e(a, cg, sig, filt, shape, world, barrier) if not a.no_e2e else None
+
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": "conv/s", "n_gpus": world, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "bf16x3" if a.path == "tc" else "f32",
+        "data": "synthetic (seeded torch generator; signals N(0,1), filters U[-1,1])",
+        "config": _config(a.path),
+        "hbm_gbs_model": round(model_bytes / (ms_step / 1e3) / 1e9, 1),
+        "roofline": roofline,
+        "passes": {k: {"ms_per_launch": round(v["ms"] / v["launches"], 4), "launches": v["launches"],
+                       "gbs": round(v["bytes"] / (v["ms"] / 1e3) / 1e9, 1)} for k, v in passes.items()},
+        "e2e": e2e,
+        "gpu_launches": gpu_launches,
+        "clocks": clocks,
+    }
+    if world == 1 and not a.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline()
+    print(json.dumps(line), flush=True)
+
+
+def _e2e(a, cg, sig, filt, shape, world, barrier):
+    import torch
+
     vol = BATCH * N ** 3
     hs = cg.PinnedBuffer.alloc(vol * 8)
     hf = cg.PinnedBuffer.alloc(vol * 8)
@@ -334,26 +364,7 @@ def run_ours(a) -> None:
            "last_call_ms": {k: round(v, 3) for k, v in t.as_dict().items() if k != "valid"}}
     for b in (hs, hf, ho):
         b.free()
-
-    if rank != 0:
-        return
-    line = {
-        "metric": METRIC, "value": value, "unit": "conv/s", "n_gpus": world, "steps": a.steps,
-        "warmup": a.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "bf16x3" if a.path == "tc" else "f32",
-        "data": "synthetic (seeded torch generator; signals N(0,1), filters U[-1,1])",
-        "config": _config(a.path),
-        "hbm_gbs_model": round(model_bytes / (ms_step / 1e3) / 1e9, 1),
-        "roofline": roofline,
-        "passes": {k: {"ms_per_launch": round(v["ms"] / v["launches"], 4), "launches": v["launches"],
-                       "gbs": round(v["bytes"] / (v["ms"] / 1e3) / 1e9, 1)} for k, v in passes.items()},
-        "e2e": e2e,
-        "gpu_launches": gpu_launches,
-        "clocks": clocks,
-    }
-    if world == 1 and not a.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline()
-    print(json.dumps(line), flush=True)
+    return e2e
 
 
 def _read_traffic(kernel: str):
