@@ -45,6 +45,7 @@ EXPORTED_SYMBOLS = (
     "fpgaf_conv3D_svm",
     "fpgaf_conv3D_svm_batch",
     "convgpu_conv3d_device",
+    "convgpu_conv3d_device_noalloc",
     "convgpu_conv3d_host",
     "convgpu_filter_spectrum_device",
     "convgpu_conv3d_uneven_device",
@@ -117,6 +118,8 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
     lib.fpgaf_conv3D_svm_batch.restype = FpgaTiming
     lib.convgpu_conv3d_device.argtypes = [u, vp, vp, vp, u, u, vp]
     lib.convgpu_conv3d_device.restype = ctypes.c_int
+    lib.convgpu_conv3d_device_noalloc.argtypes = [u, vp, vp, vp, u, u, vp]
+    lib.convgpu_conv3d_device_noalloc.restype = ctypes.c_int
     lib.convgpu_conv3d_host.argtypes = [u, vp, vp, vp, u, u]
     lib.convgpu_conv3d_host.restype = FpgaTiming
     lib.convgpu_filter_spectrum_device.argtypes = [u, vp, vp, u, vp]
@@ -215,6 +218,18 @@ def conv3d_device(n: int, sig, filt, out, how_many: int, flags: int = 0, stream=
     rc = load_library().convgpu_conv3d_device(n, _dev_ptr(sig), _dev_ptr(filt), _dev_ptr(out), how_many, flags,
                                               _stream_ptr(stream))
     _check(rc, "convgpu_conv3d_device")
+
+
+NOALLOC_SCRATCH_ELEMS = 1 << 21
+
+
+def conv3d_device_noalloc(n: int, sig, filt, out, how_many: int, flags: int = 0, stream=None) -> None:
+    """Like conv3d_device, for callers that cannot allocate device memory: its scratch
+    is a fixed 16 MiB array inside the library (NOALLOC_SCRATCH_ELEMS complex values),
+    shared by all calls (overlapping calls race). Raises on error."""
+    rc = load_library().convgpu_conv3d_device_noalloc(n, _dev_ptr(sig), _dev_ptr(filt), _dev_ptr(out), how_many,
+                                                      flags, _stream_ptr(stream))
+    _check(rc, "convgpu_conv3d_device_noalloc")
 
 
 def conv3d_host(n: int, sig, filt, out, how_many: int, flags: int = 0) -> FpgaTiming:

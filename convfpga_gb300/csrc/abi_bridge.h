@@ -34,6 +34,8 @@ int bridge_conv_device(unsigned n, const void *d_sig, const void *d_filt, void *
 int bridge_filter_spectrum_device(unsigned n, const void *d_filt, void *d_spec, unsigned count, void *stream);
 int bridge_conv_uneven_device(const UnevenJob *jobs, unsigned njobs, const void *d_sig, const void *d_filt,
                               void *d_out, unsigned flags, void *stream);
+int bridge_conv_device_noalloc(unsigned n, const void *d_sig, const void *d_filt, void *d_out, unsigned how_many,
+                               unsigned flags, void *stream);
 int bridge_workspace_bytes(unsigned n, unsigned how_many, unsigned flags, size_t *bytes);
 int bridge_device_info(int *device, int *pageable_access, int *sm_count);
 unsigned long long bridge_launch_count();

@@ -56,6 +56,11 @@ int convgpu_conv3d_device(unsigned N, const float2 *d_sig, const float2 *d_filte
   return convgpu::bridge_conv_device(N, d_sig, d_filter, d_out, how_many, flags, stream);
 }
 
+int convgpu_conv3d_device_noalloc(unsigned N, const float2 *d_sig, const float2 *d_filter, float2 *d_out,
+                                  unsigned how_many, unsigned flags, void *stream) {
+  return convgpu::bridge_conv_device_noalloc(N, d_sig, d_filter, d_out, how_many, flags, stream);
+}
+
 fpga_t convgpu_conv3d_host(unsigned N, const float2 *sig, const float2 *filter, float2 *out,
                            unsigned how_many, unsigned flags) {
   return to_fpga_t(convgpu::bridge_conv_host(N, sig, filter, out, how_many, flags, convgpu::HOST_BATCH));

@@ -51,6 +51,7 @@ static std::atomic<unsigned long long> g_launches{0};
 void count_launches(unsigned long long k) { g_launches.fetch_add(k, std::memory_order_relaxed); }
 
 static void set_err(const std::string &s) { g_err = s; }
+void record_error(const char *msg) { g_err = msg ? msg : ""; }
 static int cuda_fail(cudaError_t e, const char *what) {
   set_err(std::string(what) + ": " + cudaGetErrorString(e));
   return (e == cudaErrorMemoryAllocation) ? kErrNoMem : kErrCuda;

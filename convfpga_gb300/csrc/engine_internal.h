@@ -19,6 +19,13 @@ cudaError_t launch_axis_pass(int n, int axis, int op, const float2 *src, float2 
 // Checks that this library's kernel image loads on the current device.
 cudaError_t probe_kernel_image();
 
+// Sets the calling thread's convgpu_last_error() text.
+void record_error(const char *msg);
+
+// Entry point without device allocations (noalloc.cu); returns 0 or a CONVGPU_E* code.
+int conv_device_noalloc(unsigned n, const void *d_sig, const void *d_filt, void *d_out, unsigned how_many,
+                        unsigned flags, void *stream);
+
 // Counts kernel launches issued by this library (host-side, monotonic).
 void count_launches(unsigned long long k);
 

@@ -42,6 +42,23 @@ extern "C" {
 int convgpu_conv3d_device(unsigned N, const float2 *d_sig, const float2 *d_filter, float2 *d_out,
                           unsigned how_many, unsigned flags, void *stream);
 
+/* As convgpu_conv3d_device, but allocates no device memory: for callers that cannot
+ * call cudaMalloc, such as programs whose device memory is owned by another allocator
+ * (a framework's caching allocator, a pool sized at start-up) or steady-state loops that
+ * cannot take cudaMalloc/cudaFree's device-wide synchronisation. It has no counterpart
+ * in pc2/ConvFPGA.
+ * Scratch is a fixed 16 MiB device array inside the library (CONVGPU_NOALLOC_SCRATCH_ELEMS
+ * complex64 values), held by every GPU that loads the library until the process exits.
+ * A call needs how_many*N^3 scratch values with CONVGPU_FILTER_PER_SIGNAL, N^3 for a
+ * shared filter and none with CONVGPU_FILTER_IS_SPECTRUM; larger requests return
+ * CONVGPU_EINVAL. CONVGPU_TENSOR_SPLIT returns CONVGPU_EUNSUPPORTED.
+ * The first call on a device sets that device up (looks up the array's address and
+ * fills a twiddle table), so make it before any stream capture. All calls share the
+ * array: calls that overlap on the GPU race. */
+#define CONVGPU_NOALLOC_SCRATCH_ELEMS (1u << 21)
+int convgpu_conv3d_device_noalloc(unsigned N, const float2 *d_sig, const float2 *d_filter, float2 *d_out,
+                                  unsigned how_many, unsigned flags, void *stream);
+
 /* Host-buffer batch with the flags above (CONVGPU_TENSOR_SPLIT and
  * CONVGPU_FILTER_IS_SPECTRUM excluded). Copies overlap compute on separate streams;
  * pinned buffers (convgpu_host_alloc) copy fastest.
