@@ -56,6 +56,7 @@ EXPORTED_SYMBOLS = (
     "convgpu_launch_count",
     "convgpu_pass_timing",
     "convgpu_synchronize",
+    "convgpu_device_status",
     "convgpu_last_error",
 )
 
@@ -141,6 +142,8 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
     lib.convgpu_pass_timing.restype = ctypes.c_int
     lib.convgpu_synchronize.argtypes = []
     lib.convgpu_synchronize.restype = ctypes.c_int
+    lib.convgpu_device_status.argtypes = [ctypes.POINTER(ctypes.c_uint)]
+    lib.convgpu_device_status.restype = ctypes.c_int
     lib.convgpu_last_error.argtypes = []
     lib.convgpu_last_error.restype = ctypes.c_char_p
     if path is None:
@@ -289,6 +292,13 @@ def pass_timing_read() -> dict:
         if cnt[i]:
             out[f"{PASS_AXES[i // 4]}-{PASS_OPS[i % 4]}"] = {"ms": ms[i], "launches": int(cnt[i]), "bytes": by[i]}
     return out
+
+
+def device_status() -> int:
+    """Waits for the device; returns and clears the status word (0 = all kernels normal)."""
+    v = ctypes.c_uint(0)
+    _check(load_library().convgpu_device_status(ctypes.byref(v)), "convgpu_device_status")
+    return int(v.value)
 
 
 def synchronize() -> None:

@@ -44,5 +44,6 @@ const char *bridge_last_error();
 int bridge_host_alloc_pinned(size_t bytes, void **ptr);
 int bridge_host_free_pinned(void *ptr);
 int bridge_sync();
+int bridge_device_status(unsigned *status);
 
 }  // namespace convgpu

@@ -98,6 +98,8 @@ int convgpu_pass_timing(int mode, double *ms, unsigned long long *launches, doub
 
 int convgpu_synchronize(void) { return convgpu::bridge_sync(); }
 
+int convgpu_device_status(unsigned *status) { return convgpu::bridge_device_status(status); }
+
 const char *convgpu_last_error(void) { return convgpu::bridge_last_error(); }
 
 }  // extern "C"

@@ -166,6 +166,8 @@ static int setup_locked(int dev, bool use_svm) {
     teardown_locked();
     return -4;
   }
+  const char *no_tma = std::getenv("CONVGPU_DISABLE_TMA");
+  set_tma_enabled(!(no_tma && no_tma[0] == '1'));
   g.device = dev;
   g.use_svm = use_svm;
   g.init = true;
@@ -508,6 +510,10 @@ Timing bridge_conv_host(unsigned n, const void *sig, const void *filt, void *out
     cuda_fail(e, "host pipeline");
     return t;
   }
+  if (const unsigned st = read_and_clear_device_status()) {
+    set_err("device status " + std::to_string(st) + ": a kernel gave up waiting for its tile load");
+    return t;
+  }
   if (!per_signal) {
     t.filter_pcie_wr_t = ms_between(f0, f1);
     t.filter_exec_t = ms_between(f1, f2);
@@ -592,6 +598,17 @@ int bridge_host_free_pinned(void *ptr) {
   if (!ptr) return 0;
   cudaError_t e = cudaFreeHost(ptr);
   if (e != cudaSuccess) return cuda_fail(e, "cudaFreeHost");
+  return 0;
+}
+
+int bridge_device_status(unsigned *status) {
+  std::lock_guard<std::recursive_mutex> lk(g.mu);
+  if (!status) return kErrInval;
+  int rc = ensure_init_locked();
+  if (rc) return rc;
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) return cuda_fail(e, "synchronize");
+  *status = read_and_clear_device_status();
   return 0;
 }
 

@@ -16,6 +16,12 @@ cudaError_t launch_axis_pass(int n, int axis, int op, const float2 *src, float2 
                              long long filt_vol_elems, int nvol, float scale, const float2 *tw512,
                              cudaStream_t s);
 
+// Selects the TMA-fed y / z pass kernels (default) or the register-gather kernels.
+void set_tma_enabled(bool on);
+
+// Returns and clears the device status word (kStatus* bits; ~0 if it cannot be read).
+unsigned int read_and_clear_device_status();
+
 // Checks that this library's kernel image loads on the current device.
 cudaError_t probe_kernel_image();
 

@@ -4,12 +4,18 @@
 // reference's compile-time FFT size (kernels/common/conv_config.h.in:8-11): every
 // supported N (16..512, the reference's LOG_FFT_SIZE range 4..9) is compiled in and
 // chosen at run time.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
+
+#include <cstdint>
+#include <mutex>
 
 #include "engine_internal.h"
 #include "passes.cuh"
 
 namespace convgpu {
+
 
 template <int N>
 struct Shape;
@@ -71,6 +77,94 @@ static cudaError_t launch_shape(PassArgs a, int nvol, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+// ------------------------------------------------------------------ TMA descriptors
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    cudaDriverEntryPointQueryResult q{};
+    void *p = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    else
+      cudaGetLastError();
+  });
+  return fn;
+}
+
+// Tensor map over `nplanes` consecutive N x N planes of complex64 (8-byte elements),
+// dims (x, y, plane) = (N, N, nplanes); box {cols, 1 or nbox, nbox or 1}.
+static bool encode_cube_map(CUtensorMap *m, const void *base, int n, long long nplanes, int axis, int cols) {
+  auto enc = tensor_map_encoder();
+  if (!enc || (reinterpret_cast<uintptr_t>(base) & 15u) != 0 || nplanes > 0x7fffffffLL) return false;
+  const cuuint32_t nbox = (cuuint32_t)(n > 256 ? 256 : n);
+  cuuint64_t dims[3] = {(cuuint64_t)n, (cuuint64_t)n, (cuuint64_t)nplanes};
+  cuuint64_t strides[2] = {(cuuint64_t)n * 8, (cuuint64_t)n * n * 8};
+  cuuint32_t box[3] = {(cuuint32_t)cols, axis == 1 ? nbox : 1u, axis == 1 ? 1u : nbox};
+  cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_UINT64, 3, const_cast<void *>(base), dims, strides, box, estr,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
+// Strided pass through the TMA kernel. Returns cudaErrorNotSupported when the
+// operands cannot be described by tensor maps (unaligned pointers), so the caller can
+// use the register-gather kernel instead.
+template <int N, int OP>
+static cudaError_t launch_tma(int axis, PassArgs a, int nvol, cudaStream_t s) {
+  using S = Shape<N>;
+  constexpr int E = S::E;
+  constexpr int COLS = S::SC;
+  constexpr int threads = COLS * (N / E);
+  constexpr int smem = tma_pass_smem_bytes<N, COLS, OP>();
+  constexpr bool HAS_F = (OP == OP_CONV || OP == OP_CONV_FZ);
+  if ((reinterpret_cast<uintptr_t>(a.dst) & 15u) != 0) return cudaErrorNotSupported;
+  CUtensorMap msrc, mfilt;
+  if (!encode_cube_map(&msrc, a.src, N, (long long)nvol * N, axis, COLS)) return cudaErrorNotSupported;
+  if (HAS_F) {
+    const long long fplanes = a.filt_vol_elems ? (long long)nvol * N : (long long)N;
+    if (!encode_cube_map(&mfilt, a.filt, N, fplanes, axis, COLS)) return cudaErrorNotSupported;
+  } else {
+    mfilt = msrc;
+  }
+  auto kern = k_strided_tma<N, E, COLS, OP, typename S::Plan>;
+  static bool attr_done = false;
+  if (!attr_done) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    attr_done = true;
+  }
+  const long long blocks = (long long)nvol * a.groups_per_vol;
+  if (blocks <= 0 || blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+  kern<<<(unsigned)blocks, threads, smem, s>>>(msrc, mfilt, a, axis);
+  return cudaGetLastError();
+}
+
+template <int N>
+static cudaError_t launch_tma_op(int axis, int op, PassArgs a, int nvol, cudaStream_t s) {
+  switch (op) {
+    case OP_FWD: return launch_tma<N, OP_FWD>(axis, a, nvol, s);
+    case OP_INV: return launch_tma<N, OP_INV>(axis, a, nvol, s);
+    case OP_CONV: return launch_tma<N, OP_CONV>(axis, a, nvol, s);
+    case OP_CONV_FZ: return launch_tma<N, OP_CONV_FZ>(axis, a, nvol, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+static bool g_use_tma = true;
+void set_tma_enabled(bool on) { g_use_tma = on; }
+
+unsigned int read_and_clear_device_status() {
+  unsigned int v = 0;
+  if (cudaMemcpyFromSymbol(&v, g_device_status, sizeof(v)) != cudaSuccess) return ~0u;
+  const unsigned int zero = 0;
+  cudaMemcpyToSymbol(g_device_status, &zero, sizeof(zero));
+  return v;
+}
+
 template <int N, bool CONTIG>
 static cudaError_t launch_op(int op, PassArgs a, int nvol, cudaStream_t s) {
   switch (op) {
@@ -100,6 +194,10 @@ static cudaError_t launch_n(int axis, int op, PassArgs a, int nvol, cudaStream_t
   } else {
     a.axis_stride = (long long)N * N;
     a.plane_pitch = N;
+  }
+  if (g_use_tma) {
+    cudaError_t e = launch_tma_op<N>(axis, op, a, nvol, s);
+    if (e != cudaErrorNotSupported) return e;
   }
   return launch_op<N, false>(op, a, nvol, s);
 }

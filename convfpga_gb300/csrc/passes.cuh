@@ -24,6 +24,7 @@
 #include <cstdint>
 
 #include "fft_core.cuh"
+#include "tma.cuh"
 
 namespace convgpu {
 
@@ -161,6 +162,113 @@ __global__ void __launch_bounds__(COLS *(N / E)) k_axis_pass(PassArgs a) {
 
 #pragma unroll
   for (int e = 0; e < E; ++e) a.dst[base + (long long)(t + e * T) * es] = v[e];
+}
+
+// Device status word: kernels OR in kStatus* bits when a bounded wait gives up. Only
+// passes.cu instantiates kernels and reads it back; other translation units that include
+// this header never touch their copy.
+static __device__ unsigned int g_device_status;
+
+// Dynamic shared memory of the TMA-fed strided pass: barrier (128 B slot), the signal
+// tile, the filter tile (fused z ops), then N twiddles.
+template <int N, int COLS, int OP>
+constexpr int tma_pass_smem_bytes() {
+  return 128 + N * COLS * 8 * ((OP == OP_CONV || OP == OP_CONV_FZ) ? 2 : 1) + N * 8;
+}
+
+// y / z pass fed by TMA. One CTA owns COLS adjacent x-columns of one plane (y pass,
+// axis 1) or one row (z pass, axis 2): thread 0 loads the whole N x COLS tile (and the
+// matching filter tile for the fused z ops) with cp.async.bulk.tensor into shared memory,
+// position-major with columns contiguous -- exactly the ColSlot layout the Stockham
+// stages exchange through, so the tile buffer doubles as the exchange buffer. The
+// filter operand never occupies registers; CONV_FZ transforms it in place in its tile.
+// Boxes are at most 256 long, so N = 512 takes two loads per tile.
+template <int N, int E, int COLS, int OP, class Plan>
+__global__ void __launch_bounds__(COLS *(N / E)) k_strided_tma(const __grid_constant__ CUtensorMap msrc,
+                                                              const __grid_constant__ CUtensorMap mfilt,
+                                                              PassArgs a, int axis) {
+  constexpr int T = N / E;
+  constexpr bool HAS_F = (OP == OP_CONV || OP == OP_CONV_FZ);
+  constexpr int TILE = N * COLS;
+  constexpr int NBOX = N > 256 ? 256 : N;
+  constexpr int NLOADS = N / NBOX;
+  extern __shared__ __align__(128) unsigned char smraw[];
+  float2 *tile = reinterpret_cast<float2 *>(smraw + 128);
+  float2 *ftile = tile + TILE;
+  float2 *tw = HAS_F ? ftile + TILE : tile + TILE;
+  const uint32_t bar = smem_u32(smraw);
+
+  const int vol = blockIdx.x / a.groups_per_vol;
+  const int r = blockIdx.x % a.groups_per_vol;
+  const int row = r / a.groups_x;  // z of the plane (y pass) or y of the row (z pass)
+  const int x0 = (r % a.groups_x) * COLS;
+
+  if (threadIdx.x == 0) {
+    mbar_init(bar, 1);
+    mbar_fence_init();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    mbar_arrive_expect_tx(bar, (HAS_F ? 2u : 1u) * TILE * 8u);
+#pragma unroll
+    for (int l = 0; l < NLOADS; ++l) {
+      if (axis == 1)
+        tma_load_3d(smem_u32(tile + l * NBOX * COLS), &msrc, x0, l * NBOX, vol * N + row, bar);
+      else
+        tma_load_3d(smem_u32(tile + l * NBOX * COLS), &msrc, x0, row, vol * N + l * NBOX, bar);
+      if constexpr (HAS_F) {
+        const int fv = a.filt_vol_elems ? vol : 0;
+        tma_load_3d(smem_u32(ftile + l * NBOX * COLS), &mfilt, x0, row, fv * N + l * NBOX, bar);
+      }
+    }
+  }
+  for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = a.tw512[i * (512 / N)];
+  const int c = threadIdx.x % COLS;
+  const int t = threadIdx.x / COLS;
+  const ColSlot<COLS> sidx{c};
+  // Uniform decision: every thread takes the same branch, so no barrier is left waiting.
+  const int ok = __syncthreads_and(mbar_wait_bounded(bar, 0) ? 1 : 0);
+  if (!ok) {
+    if (threadIdx.x == 0) atomicOr(&g_device_status, kStatusTmaTimeout);
+    mbar_wait_bounded(bar, 0);  // let copies still in flight land before the CTA exits
+    return;
+  }
+
+  float2 v[E];
+  if constexpr (OP == OP_CONV_FZ) {
+    float2 f[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) f[e] = ftile[sidx(t + e * T)];
+    __syncthreads();
+    fft_forward<N, E>(f, t, tw, ftile, sidx, Plan{});
+#pragma unroll
+    for (int e = 0; e < E; ++e) ftile[sidx(t + e * T)] = f[e];  // own slots: read back by this thread only
+  }
+#pragma unroll
+  for (int e = 0; e < E; ++e) v[e] = tile[sidx(t + e * T)];
+  __syncthreads();
+
+  if constexpr (OP == OP_FWD) {
+    fft_forward<N, E>(v, t, tw, tile, sidx, Plan{});
+  } else if constexpr (OP == OP_INV) {
+    swap_all(v);
+    fft_forward<N, E>(v, t, tw, tile, sidx, Plan{});
+    swap_all(v);
+  } else {
+    fft_forward<N, E>(v, t, tw, tile, sidx, Plan{});
+#pragma unroll
+    for (int e = 0; e < E; ++e) v[e] = cmul(v[e], ftile[sidx(t + e * T)]);
+    swap_all(v);
+    fft_forward<N, E>(v, t, tw, tile, sidx, Plan{});
+    swap_all(v);
+  }
+  if (a.scale != 1.0f) {
+#pragma unroll
+    for (int e = 0; e < E; ++e) v[e] = make_float2(v[e].x * a.scale, v[e].y * a.scale);
+  }
+  float2 *dst = a.dst + (long long)vol * a.vol_elems + (long long)row * a.plane_pitch + x0 + c;
+#pragma unroll
+  for (int e = 0; e < E; ++e) dst[(long long)(t + e * T) * a.axis_stride] = v[e];
 }
 
 }  // namespace convgpu

@@ -114,6 +114,11 @@ int convgpu_pass_timing(int mode, double *ms, unsigned long long *launches, doub
 /* Waits for all work on the library's device. */
 int convgpu_synchronize(void);
 
+/* Waits for the device, then returns and clears the library's device status word in
+ * *status: 0 when every kernel completed normally; bit 0 set when a kernel gave up a
+ * bounded wait for its tile load (it then wrote no output for that tile). */
+int convgpu_device_status(unsigned *status);
+
 /* Text of the calling thread's last error ("" if none). */
 const char *convgpu_last_error(void);
 
