@@ -110,6 +110,45 @@ static bool encode_cube_map(CUtensorMap *m, const void *base, int n, long long n
   return r == CUDA_SUCCESS;
 }
 
+// Tensor map over `rows` rows of N complex64: dims (x, row) = (N, rows), box
+// {min(N,256), xc}.
+static bool encode_rows_map(CUtensorMap *m, const void *base, int n, long long rows, int xc) {
+  auto enc = tensor_map_encoder();
+  if (!enc || (reinterpret_cast<uintptr_t>(base) & 15u) != 0 || rows > 0x7fffffffLL) return false;
+  cuuint64_t dims[2] = {(cuuint64_t)n, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)n * 8};
+  cuuint32_t box[2] = {(cuuint32_t)(n > 256 ? 256 : n), (cuuint32_t)xc};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_UINT64, 2, const_cast<void *>(base), dims, strides, box, estr,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
+template <int N, int OP>
+static cudaError_t launch_rows_tma(PassArgs a, int nvol, cudaStream_t s) {
+  using S = Shape<N>;
+  constexpr int E = S::E;
+  constexpr int XC = S::XC;
+  constexpr int threads = XC * (N / E);
+  constexpr int smem = tma_rows_smem_bytes<N, XC>();
+  if ((reinterpret_cast<uintptr_t>(a.dst) & 15u) != 0) return cudaErrorNotSupported;
+  const long long rows = (long long)nvol * N * N;
+  CUtensorMap msrc;
+  if (!encode_rows_map(&msrc, a.src, N, rows, XC)) return cudaErrorNotSupported;
+  auto kern = k_rows_tma<N, E, XC, OP, typename S::Plan>;
+  static bool attr_done = false;
+  if (!attr_done) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    attr_done = true;
+  }
+  const long long blocks = rows / XC;
+  if (blocks <= 0 || blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+  kern<<<(unsigned)blocks, threads, smem, s>>>(msrc, a);
+  return cudaGetLastError();
+}
+
 // Strided pass through the TMA kernel. Returns cudaErrorNotSupported when the
 // operands cannot be described by tensor maps (unaligned pointers), so the caller can
 // use the register-gather kernel instead.
@@ -186,7 +225,13 @@ static cudaError_t launch_n(int axis, int op, PassArgs a, int nvol, cudaStream_t
   constexpr int SC = Shape<N>::SC;
   a.vol_elems = (long long)N * N * N;
   a.groups_x = N / SC;
-  if (axis == 0) return launch_op<N, true>(op, a, nvol, s);
+  if (axis == 0) {
+    if (g_use_tma && (op == OP_FWD || op == OP_INV)) {
+      cudaError_t e = op == OP_FWD ? launch_rows_tma<N, OP_FWD>(a, nvol, s) : launch_rows_tma<N, OP_INV>(a, nvol, s);
+      if (e != cudaErrorNotSupported) return e;
+    }
+    return launch_op<N, true>(op, a, nvol, s);
+  }
   a.groups_per_vol = N * (N / SC);
   if (axis == 1) {
     a.axis_stride = N;

@@ -169,6 +169,21 @@ __global__ void __launch_bounds__(COLS *(N / E)) k_axis_pass(PassArgs a) {
 // this header never touch their copy.
 static __device__ unsigned int g_device_status;
 
+// Dynamic shared memory of the TMA-fed x pass: barrier slot, the unpadded row tile (TMA
+// target), the padded exchange buffer, then N twiddles.
+template <int N, int XC>
+constexpr int tma_rows_smem_bytes() {
+  return 128 + XC * N * 8 + XC * row_pitch<N>() * 8 + N * 8;
+}
+
+// Slot of element n of tile row c as TMA lands it: boxes are at most 256 wide, so a
+// 512-point row arrives as two half-tiles [half][row][256].
+template <int N, int XC>
+__device__ __forceinline__ int rowtile_idx(int c, int n) {
+  if constexpr (N <= 256) return c * N + n;
+  else return ((n >> 8) * XC + c) * 256 + (n & 255);
+}
+
 // Dynamic shared memory of the TMA-fed strided pass: barrier (128 B slot), the signal
 // tile, the filter tile (fused z ops), then N twiddles.
 template <int N, int COLS, int OP>
@@ -269,6 +284,59 @@ __global__ void __launch_bounds__(COLS *(N / E)) k_strided_tma(const __grid_cons
   float2 *dst = a.dst + (long long)vol * a.vol_elems + (long long)row * a.plane_pitch + x0 + c;
 #pragma unroll
   for (int e = 0; e < E; ++e) dst[(long long)(t + e * T) * a.axis_stride] = v[e];
+}
+
+// x pass fed by TMA: thread 0 loads XC consecutive rows (XC*N*8 contiguous bytes) with
+// one 2D bulk-tensor copy per 256-wide box; threads read their t + e*T elements
+// (consecutive lanes, consecutive slots), run the Stockham stages through the padded
+// exchange buffer and store straight to global memory.
+template <int N, int E, int XC, int OP, class Plan>
+__global__ void __launch_bounds__(XC *(N / E)) k_rows_tma(const __grid_constant__ CUtensorMap msrc, PassArgs a) {
+  static_assert(OP == OP_FWD || OP == OP_INV, "x pass ops");
+  constexpr int T = N / E;
+  constexpr int NBOX = N > 256 ? 256 : N;
+  constexpr int NLOADS = N / NBOX;
+  extern __shared__ __align__(128) unsigned char smraw[];
+  float2 *tile = reinterpret_cast<float2 *>(smraw + 128);
+  float2 *exch = tile + XC * N;
+  float2 *tw = exch + XC * row_pitch<N>();
+  const uint32_t bar = smem_u32(smraw);
+  const long long row0 = (long long)blockIdx.x * XC;
+
+  if (threadIdx.x == 0) {
+    mbar_init(bar, 1);
+    mbar_fence_init();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    mbar_arrive_expect_tx(bar, (uint32_t)(XC * N * 8));
+#pragma unroll
+    for (int l = 0; l < NLOADS; ++l)
+      tma_load_2d(smem_u32(tile + l * XC * NBOX), &msrc, l * NBOX, (int)row0, bar);
+  }
+  for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = a.tw512[i * (512 / N)];
+  const int t = threadIdx.x % T;
+  const int c = threadIdx.x / T;
+  const RowSlot<N> sidx{c * row_pitch<N>()};
+  const int ok = __syncthreads_and(mbar_wait_bounded(bar, 0) ? 1 : 0);
+  if (!ok) {
+    if (threadIdx.x == 0) atomicOr(&g_device_status, kStatusTmaTimeout);
+    mbar_wait_bounded(bar, 0);
+    return;
+  }
+  float2 v[E];
+#pragma unroll
+  for (int e = 0; e < E; ++e) v[e] = tile[rowtile_idx<N, XC>(c, t + e * T)];
+  if constexpr (OP == OP_INV) swap_all(v);
+  fft_forward<N, E>(v, t, tw, exch, sidx, Plan{});
+  if constexpr (OP == OP_INV) swap_all(v);
+  if (a.scale != 1.0f) {
+#pragma unroll
+    for (int e = 0; e < E; ++e) v[e] = make_float2(v[e].x * a.scale, v[e].y * a.scale);
+  }
+  float2 *dst = a.dst + (row0 + c) * N + t;
+#pragma unroll
+  for (int e = 0; e < E; ++e) dst[e * T] = v[e];
 }
 
 }  // namespace convgpu
