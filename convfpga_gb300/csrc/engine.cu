@@ -38,6 +38,7 @@ constexpr unsigned kFlagNormalize = 1u << 0;
 constexpr unsigned kFlagPerSignalFilter = 1u << 1;
 constexpr unsigned kFlagFilterIsSpectrum = 1u << 2;
 constexpr unsigned kFlagTensorSplit = 1u << 3;
+constexpr unsigned kFlagTensorBf16x3 = 1u << 4;
 
 constexpr int kErrInval = -1;
 constexpr int kErrNotInit = -2;
@@ -199,7 +200,7 @@ static bool g_prof = false;
 static std::vector<PassRec> g_prof_recs;
 
 static cudaError_t pass(int n, int axis, int op, const float2 *src, float2 *dst, const float2 *filt,
-                        long long filt_vol, int nvol, float scale, cudaStream_t s) {
+                        long long filt_vol, int nvol, float scale, cudaStream_t s, int tc) {
   PassRec r{axis * 4 + op, 0.0, nullptr, nullptr};
   if (g_prof) {
     const double vol = (double)n * n * n * 8.0 * nvol;
@@ -208,7 +209,8 @@ static cudaError_t pass(int n, int axis, int op, const float2 *src, float2 *dst,
     cudaEventCreate(&r.b);
     cudaEventRecord(r.a, s);
   }
-  cudaError_t e = launch_axis_pass(n, axis, op, src, dst, filt, filt_vol, nvol, scale, g.tw512, s);
+  cudaError_t e = tc ? launch_axis_pass_tc(n, axis, op, src, dst, filt, filt_vol, nvol, scale, g.tw512, s, tc - 1)
+                     : launch_axis_pass(n, axis, op, src, dst, filt, filt_vol, nvol, scale, g.tw512, s);
   if (g_prof) {
     cudaEventRecord(r.b, s);
     g_prof_recs.push_back(r);
@@ -226,10 +228,10 @@ static cudaError_t pass(int n, int axis, int op, const float2 *src, float2 *dst,
 
 // Filter spectra of `count` filters (x, y and, unless xy_only, z passes) into spec.
 static cudaError_t enqueue_filter(int n, const float2 *filt, float2 *spec, int count, bool xy_only,
-                                  cudaStream_t s) {
-  CG_TRY(pass(n, 0, OP_FWD, filt, spec, nullptr, 0, count, 1.f, s));
-  CG_TRY(pass(n, 1, OP_FWD, spec, spec, nullptr, 0, count, 1.f, s));
-  if (!xy_only) CG_TRY(pass(n, 2, OP_FWD, spec, spec, nullptr, 0, count, 1.f, s));
+                                  cudaStream_t s, int tc = 0) {
+  CG_TRY(pass(n, 0, OP_FWD, filt, spec, nullptr, 0, count, 1.f, s, tc));
+  CG_TRY(pass(n, 1, OP_FWD, spec, spec, nullptr, 0, count, 1.f, s, tc));
+  if (!xy_only) CG_TRY(pass(n, 2, OP_FWD, spec, spec, nullptr, 0, count, 1.f, s, tc));
   return cudaSuccess;
 }
 
@@ -237,13 +239,13 @@ static cudaError_t enqueue_filter(int n, const float2 *filt, float2 *spec, int c
 // mid (optional) is recorded after the fused z pass.
 static cudaError_t enqueue_signals(int n, const float2 *sig, float2 *out, const float2 *spec,
                                    long long spec_vol, int fop, int nsig, float scale, cudaStream_t s,
-                                   cudaEvent_t mid) {
-  CG_TRY(pass(n, 0, OP_FWD, sig, out, nullptr, 0, nsig, 1.f, s));
-  CG_TRY(pass(n, 1, OP_FWD, out, out, nullptr, 0, nsig, 1.f, s));
-  CG_TRY(pass(n, 2, fop, out, out, spec, spec_vol, nsig, 1.f, s));
+                                   cudaEvent_t mid, int tc = 0) {
+  CG_TRY(pass(n, 0, OP_FWD, sig, out, nullptr, 0, nsig, 1.f, s, tc));
+  CG_TRY(pass(n, 1, OP_FWD, out, out, nullptr, 0, nsig, 1.f, s, tc));
+  CG_TRY(pass(n, 2, fop, out, out, spec, spec_vol, nsig, 1.f, s, tc));
   if (mid) cudaEventRecord(mid, s);
-  CG_TRY(pass(n, 1, OP_INV, out, out, nullptr, 0, nsig, 1.f, s));
-  CG_TRY(pass(n, 0, OP_INV, out, out, nullptr, 0, nsig, scale, s));
+  CG_TRY(pass(n, 1, OP_INV, out, out, nullptr, 0, nsig, 1.f, s, tc));
+  CG_TRY(pass(n, 0, OP_INV, out, out, nullptr, 0, nsig, scale, s, tc));
   return cudaSuccess;
 }
 
@@ -259,18 +261,22 @@ static cudaError_t enqueue_conv_device(unsigned n, const float2 *sig, const floa
                                        unsigned how_many, unsigned flags, float2 *ws, cudaStream_t s) {
   const float scale = (flags & kFlagNormalize) ? (float)(1.0 / ((double)n * n * n)) : 1.0f;
   const long long V = (long long)n * n * n;
+  // 0: FP32 kernels; 1 + split precision for the tensor-core path.
+  const int tc = (flags & (kFlagTensorSplit | kFlagTensorBf16x3))
+                     ? 1 + ((flags & kFlagTensorBf16x3) ? kTcBf16x3 : kTcTf32x3)
+                     : 0;
   if (flags & kFlagFilterIsSpectrum) {
     const long long sv = (flags & kFlagPerSignalFilter) ? V : 0;
-    return enqueue_signals(n, sig, out, filt, sv, OP_CONV, how_many, scale, s, nullptr);
+    return enqueue_signals(n, sig, out, filt, sv, OP_CONV, how_many, scale, s, nullptr, tc);
   }
   if (flags & kFlagPerSignalFilter) {
-    cudaError_t e = enqueue_filter(n, filt, ws, how_many, true, s);
+    cudaError_t e = enqueue_filter(n, filt, ws, how_many, true, s, tc);
     if (e != cudaSuccess) return e;
-    return enqueue_signals(n, sig, out, ws, V, OP_CONV_FZ, how_many, scale, s, nullptr);
+    return enqueue_signals(n, sig, out, ws, V, OP_CONV_FZ, how_many, scale, s, nullptr, tc);
   }
-  cudaError_t e = enqueue_filter(n, filt, ws, 1, false, s);
+  cudaError_t e = enqueue_filter(n, filt, ws, 1, false, s, tc);
   if (e != cudaSuccess) return e;
-  return enqueue_signals(n, sig, out, ws, 0, OP_CONV, how_many, scale, s, nullptr);
+  return enqueue_signals(n, sig, out, ws, 0, OP_CONV, how_many, scale, s, nullptr, tc);
 }
 
 // ------------------------------------------------------------------ bridge: setup
@@ -327,10 +333,6 @@ int bridge_conv_device(unsigned n, const void *d_sig, const void *d_filt, void *
     return kErrInval;
   }
   if (how_many == 0) return 0;
-  if (flags & kFlagTensorSplit) {
-    set_err("tensor-core split path not available in this build");
-    return kErrUnsupported;
-  }
   std::lock_guard<std::recursive_mutex> lk(g.mu);
   int rc = ensure_init_locked();
   if (rc) return rc;
@@ -418,10 +420,14 @@ Timing bridge_conv_host(unsigned n, const void *sig, const void *filt, void *out
     set_err("how_many is 0");
     return t;
   }
-  if (flags & (kFlagTensorSplit | kFlagFilterIsSpectrum)) {
-    set_err("flag not supported by the host-buffer entry points");
+  if (flags & kFlagFilterIsSpectrum) {
+    set_err("CONVGPU_FILTER_IS_SPECTRUM is not supported by the host-buffer entry points");
     return t;
   }
+  // 0: FP32 kernels; 1 + split precision for the tensor-core path.
+  const int tc = (flags & (kFlagTensorSplit | kFlagTensorBf16x3))
+                     ? 1 + ((flags & kFlagTensorBf16x3) ? kTcBf16x3 : kTcTf32x3)
+                     : 0;
   std::lock_guard<std::recursive_mutex> lk(g.mu);
   if (ensure_init_locked() != 0) return t;
   (void)mode;
@@ -467,7 +473,7 @@ Timing bridge_conv_host(unsigned n, const void *sig, const void *filt, void *out
     e = cudaMemcpyAsync(fspec, filt, vbytes, cudaMemcpyHostToDevice, g.sh2d);
     cudaEventRecord(f1, g.sh2d);
     cudaStreamWaitEvent(g.sc, f1, 0);
-    if (e == cudaSuccess) e = enqueue_filter(n, fspec, fspec, 1, false, g.sc);
+    if (e == cudaSuccess) e = enqueue_filter(n, fspec, fspec, 1, false, g.sc, tc);
     cudaEventRecord(f2, g.sc);
   }
 
@@ -487,12 +493,12 @@ Timing bridge_conv_host(unsigned n, const void *sig, const void *filt, void *out
     cudaStreamWaitEvent(g.sc, h1[c], 0);
     cudaEventRecord(c0[c], g.sc);
     if (per_signal) {
-      e = enqueue_filter(n, (const float2 *)g.hfio[b].p, (float2 *)g.hfio[b].p, cnt, true, g.sc);
+      e = enqueue_filter(n, (const float2 *)g.hfio[b].p, (float2 *)g.hfio[b].p, cnt, true, g.sc, tc);
       if (e == cudaSuccess)
         e = enqueue_signals(n, io, io, (const float2 *)g.hfio[b].p, (long long)V, OP_CONV_FZ, cnt, scale, g.sc,
-                            cm[c]);
+                            cm[c], tc);
     } else {
-      e = enqueue_signals(n, io, io, fspec, 0, OP_CONV, cnt, scale, g.sc, cm[c]);
+      e = enqueue_signals(n, io, io, fspec, 0, OP_CONV, cnt, scale, g.sc, cm[c], tc);
     }
     cudaEventRecord(c1[c], g.sc);
     if (e != cudaSuccess) break;

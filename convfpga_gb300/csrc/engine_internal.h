@@ -16,6 +16,16 @@ cudaError_t launch_axis_pass(int n, int axis, int op, const float2 *src, float2 
                              long long filt_vol_elems, int nvol, float scale, const float2 *tw512,
                              cudaStream_t s);
 
+// Split precision of the tensor-core path.
+constexpr int kTcTf32x3 = 0;
+constexpr int kTcBf16x3 = 1;
+
+// As launch_axis_pass, with the radix-16 stages on the tensor cores (split operands,
+// FP32 accumulate) where a tensor-core kernel exists (N = 256); FP32 kernels otherwise.
+cudaError_t launch_axis_pass_tc(int n, int axis, int op, const float2 *src, float2 *dst, const float2 *filt,
+                                long long filt_vol_elems, int nvol, float scale, const float2 *tw512,
+                                cudaStream_t s, int prec);
+
 // Selects the TMA-fed y / z pass kernels (default) or the register-gather kernels.
 void set_tma_enabled(bool on);
 

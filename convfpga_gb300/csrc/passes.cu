@@ -13,6 +13,7 @@
 
 #include "engine_internal.h"
 #include "passes.cuh"
+#include "tc.cuh"
 
 namespace convgpu {
 
@@ -268,6 +269,90 @@ cudaError_t launch_axis_pass(int n, int axis, int op, const float2 *src, float2 
     case 512: return launch_n<512>(axis, op, a, nvol, s);
     default: return cudaErrorInvalidValue;
   }
+}
+
+// ------------------------------------------------------------------ tensor-core path
+template <class P, int OP>
+static cudaError_t launch_tc256(int axis, PassArgs a, int nvol, cudaStream_t s) {
+  constexpr int N = 256;
+  if ((reinterpret_cast<uintptr_t>(a.dst) & 15u) != 0) return cudaErrorNotSupported;
+  if (axis == 0) {
+    if constexpr (OP == OP_FWD || OP == OP_INV) {
+      constexpr int XC = 16;
+      constexpr int smem = 128 + XC * N * 8 + XC * 272 * 8 + N * 8;
+      CUtensorMap m;
+      const long long rows = (long long)nvol * N * N;
+      if (!encode_rows_map(&m, a.src, N, rows, XC)) return cudaErrorNotSupported;
+      auto kern = k_rows_tma_tc256<P, OP>;
+      static bool attr_done = false;
+      if (!attr_done) {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) return e;
+        attr_done = true;
+      }
+      kern<<<(unsigned)(rows / XC), 256, smem, s>>>(m, a);
+      return cudaGetLastError();
+    }
+    return cudaErrorInvalidValue;
+  }
+  constexpr int smem = tma_pass_smem_bytes<N, 16, OP>();
+  constexpr bool HAS_F = (OP == OP_CONV || OP == OP_CONV_FZ);
+  CUtensorMap msrc, mfilt;
+  if (!encode_cube_map(&msrc, a.src, N, (long long)nvol * N, axis, 16)) return cudaErrorNotSupported;
+  if (HAS_F) {
+    const long long fplanes = a.filt_vol_elems ? (long long)nvol * N : (long long)N;
+    if (!encode_cube_map(&mfilt, a.filt, N, fplanes, axis, 16)) return cudaErrorNotSupported;
+  } else {
+    mfilt = msrc;
+  }
+  auto kern = k_strided_tma_tc256<P, OP>;
+  static bool attr_done = false;
+  if (!attr_done) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    attr_done = true;
+  }
+  const long long blocks = (long long)nvol * a.groups_per_vol;
+  kern<<<(unsigned)blocks, 256, smem, s>>>(msrc, mfilt, a, axis);
+  return cudaGetLastError();
+}
+
+template <class P>
+static cudaError_t launch_tc256_op(int op, int axis, PassArgs a, int nvol, cudaStream_t s) {
+  switch (op) {
+    case OP_FWD: return launch_tc256<P, OP_FWD>(axis, a, nvol, s);
+    case OP_INV: return launch_tc256<P, OP_INV>(axis, a, nvol, s);
+    case OP_CONV: return launch_tc256<P, OP_CONV>(axis, a, nvol, s);
+    case OP_CONV_FZ: return launch_tc256<P, OP_CONV_FZ>(axis, a, nvol, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t launch_axis_pass_tc(int n, int axis, int op, const float2 *src, float2 *dst, const float2 *filt,
+                                long long filt_vol_elems, int nvol, float scale, const float2 *tw512,
+                                cudaStream_t s, int prec) {
+  // The tensor-core kernels cover N = 256 (two radix-16 stages per axis); other sizes,
+  // and operands that tensor maps cannot describe, run the FP32 kernels.
+  if (n != 256 || nvol <= 0 || !g_use_tma)
+    return launch_axis_pass(n, axis, op, src, dst, filt, filt_vol_elems, nvol, scale, tw512, s);
+  if ((op == OP_CONV || op == OP_CONV_FZ) && axis != 2) return cudaErrorInvalidValue;
+  PassArgs a{};
+  a.src = src;
+  a.dst = dst;
+  a.filt = filt;
+  a.tw512 = tw512;
+  a.filt_vol_elems = filt_vol_elems;
+  a.scale = scale;
+  a.vol_elems = 256LL * 256 * 256;
+  a.groups_x = 256 / 16;
+  a.groups_per_vol = 256 * (256 / 16);
+  a.axis_stride = axis == 1 ? 256 : 256LL * 256;
+  a.plane_pitch = axis == 1 ? 256LL * 256 : 256;
+  const cudaError_t e = prec == kTcBf16x3 ? launch_tc256_op<PrecBf16x3>(op, axis, a, nvol, s)
+                                           : launch_tc256_op<PrecTf32x3>(op, axis, a, nvol, s);
+  if (e == cudaErrorNotSupported)
+    return launch_axis_pass(n, axis, op, src, dst, filt, filt_vol_elems, nvol, scale, tw512, s);
+  return e;
 }
 
 cudaError_t probe_kernel_image() {

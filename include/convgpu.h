@@ -23,7 +23,8 @@ extern "C" {
 #define CONVGPU_NORMALIZE (1u << 0)            /* scale outputs by 1/N^3 */
 #define CONVGPU_FILTER_PER_SIGNAL (1u << 1)    /* filter holds how_many cubes, one per signal */
 #define CONVGPU_FILTER_IS_SPECTRUM (1u << 2)   /* filter already holds FFT3(filter) */
-#define CONVGPU_TENSOR_SPLIT (1u << 3)         /* tensor-core split-precision path */
+#define CONVGPU_TENSOR_SPLIT (1u << 3)         /* tensor-core path, split TF32 (TF32x3) */
+#define CONVGPU_TENSOR_BF16X3 (1u << 4)        /* tensor-core path, BF16x3 split (implies TENSOR_SPLIT) */
 
 /* Status codes */
 #define CONVGPU_OK 0
@@ -37,6 +38,10 @@ extern "C" {
  * Extends fpgaf_conv3D_svm_batch (host/include/convfpga/convfpga.h:46) with device
  * buffers, per-signal filters (CONVGPU_FILTER_PER_SIGNAL), precomputed spectra
  * (CONVGPU_FILTER_IS_SPECTRUM), normalisation and the tensor-core path.
+ * Tensor-core path: the radix-16 stages of N = 256 transforms run as 16-point DFT
+ * matmuls on the tensor cores with split operands and FP32 accumulation (TF32x3:
+ * ~1e-7 relative error per 256-point transform; BF16x3: ~4e-6, which exceeds 1e-5
+ * relative L2 end to end on 256^3 convolutions). Other N run the FP32 kernels.
  * d_sig may equal d_out (in place). The library's per-device workspace is shared by
  * all calls: calls on different streams must not overlap. */
 int convgpu_conv3d_device(unsigned N, const float2 *d_sig, const float2 *d_filter, float2 *d_out,
