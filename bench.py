@@ -48,6 +48,9 @@ def _args():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling runs)")
     p.add_argument("--batch", type=int, default=BATCH, help="cubes per step (profiling runs use 1)")
+    p.add_argument("--workload", choices=["c256x4", "uneven96"], default="c256x4",
+                   help="c256x4: the headline 256^3 x4 workload; uneven96: 96 convolutions of sizes "
+                        "32..256 (work-queue launch vs one job at a time)")
     a = p.parse_args()
     a.warmup = max(a.warmup, 3)
     return a
@@ -367,6 +370,78 @@ def _e2e(a, cg, sig, filt, shape, world, barrier):
     return e2e
 
 
+def run_uneven(a) -> None:
+    """96 convolutions with sizes drawn (seed 4) from {32,64,128,256} with p = {.4,.3,.2,.1},
+    complex64 signals U[-1,1] and real Gaussian filters (sigma U[1,8]) - the same draw as the
+    oracle's generator. One step = all 96 convolutions."""
+    import numpy as np
+    import torch
+
+    import convfpga_gb300 as cg
+
+    torch.cuda.set_device(0)
+    if not os.path.exists(cg.LIB_PATH):
+        from convfpga_gb300 import build
+
+        build.build()
+    rc = cg.fpga_initialize("cuda:0", "convgpu_plans.json", False)
+    if rc != 0:
+        raise SystemExit(f"fpga_initialize failed: {rc} {cg.last_error()}")
+    sizes = [int(v) for v in np.random.default_rng(4).choice([32, 64, 128, 256], size=96, p=[.4, .3, .2, .1])]
+    offs = np.cumsum([0] + [n ** 3 for n in sizes])
+    total = int(offs[-1])
+    g = torch.Generator(device="cuda").manual_seed(99)
+    sig = torch.complex(torch.rand(total, device="cuda", generator=g) * 2 - 1,
+                        torch.rand(total, device="cuda", generator=g) * 2 - 1)
+    filt = torch.empty(total, dtype=torch.complex64, device="cuda")
+    sigmas = np.random.default_rng(5).uniform(1.0, 8.0, size=len(sizes))
+    for i, n in enumerate(sizes):
+        d = torch.arange(n, device="cuda", dtype=torch.float64)
+        d = torch.minimum(d, n - d)
+        g1 = torch.exp(-0.5 * (d / sigmas[i]) ** 2)
+        gg = (g1[:, None, None] * g1[None, :, None] * g1[None, None, :]).to(torch.float32)
+        filt[offs[i]:offs[i + 1]] = torch.complex(gg, torch.zeros_like(gg)).reshape(-1)
+    out = torch.empty_like(sig)
+    jobs = [(n, int(offs[i]), int(offs[i]), int(offs[i])) for i, n in enumerate(sizes)]
+    stream = torch.cuda.current_stream()
+
+    def timed(flags):
+        for _ in range(a.warmup):
+            cg.conv3d_uneven_device(jobs, sig, filt, out, flags, stream)
+        torch.cuda.synchronize()
+        l0 = cg.launch_count()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(a.steps):
+            cg.conv3d_uneven_device(jobs, sig, filt, out, flags, stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / a.steps, cg.launch_count() - l0
+
+    sampler = ClockSampler(0)
+    sampler.start()
+    ms_q, launches_q = timed(0)
+    clocks = sampler.stop()
+    ms_j, launches_j = timed(cg.UNEVEN_PER_JOB)
+    status = cg.device_status()
+    model = sum(136 * n ** 3 for n in sizes)
+    line = {
+        "metric": "3D FFT-conv/s, uneven batch of 96 (sizes 32..256), work-queue launch + CUDA graph",
+        "value": len(sizes) / (ms_q / 1e3), "unit": "conv/s", "n_gpus": 1, "steps": a.steps, "warmup": a.warmup,
+        "ms_per_step": ms_q, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded)",
+        "config": {"workload": "uneven96: 96 convolutions, sizes from {32,64,128,256} p={.4,.3,.2,.1} (seed 4), "
+                               "real Gaussian filters sigma U[1,8]",
+                   "size_counts": {str(n): sizes.count(n) for n in (32, 64, 128, 256)},
+                   "l2": f"no flush: each step reads {2 * total * 8 / 2**30:.2f} GiB of inputs (> 129 MB L2)"},
+        "hbm_gbs_model": round(model / (ms_q / 1e3) / 1e9, 1),
+        "per_job": {"value": len(sizes) / (ms_j / 1e3), "ms_per_step": ms_j, "gpu_launches_per_step": launches_j / a.steps},
+        "queue_speedup_vs_per_job": ms_j / ms_q,
+        "gpu_launches": launches_q, "device_status": status, "clocks": clocks,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def _read_traffic(kernel: str):
     """DRAM bytes per launch of the dominant kernel from the committed ncu summary, if any."""
     try:
@@ -379,6 +454,9 @@ def _read_traffic(kernel: str):
 
 def main():
     a = _args()
+    if a.workload == "uneven96" and a.impl == "ours":
+        run_uneven(a)
+        return
     if a.impl == "reference":
         run_reference(a)
     else:

@@ -34,6 +34,7 @@ FILTER_PER_SIGNAL = 1 << 1
 FILTER_IS_SPECTRUM = 1 << 2
 TENSOR_SPLIT = 1 << 3
 TENSOR_BF16X3 = 1 << 4
+UNEVEN_PER_JOB = 1 << 5
 
 OK, EINVAL, ENOTINIT, ECUDA, ENOMEM, EUNSUPPORTED = 0, -1, -2, -3, -4, -5
 

@@ -20,7 +20,7 @@ struct Timing {
 // Host-buffer entry points: how the reference's three conv functions map.
 enum HostMode : int { HOST_PLAIN = 0, HOST_SVM = 1, HOST_BATCH = 2 };
 
-struct UnevenJob {
+struct UnevenJob {  // layout of convgpu_job (include/convgpu.h)
   unsigned n;
   unsigned long long sig_off, filt_off, out_off;  // element offsets from the base pointers
 };

@@ -39,6 +39,7 @@ constexpr unsigned kFlagPerSignalFilter = 1u << 1;
 constexpr unsigned kFlagFilterIsSpectrum = 1u << 2;
 constexpr unsigned kFlagTensorSplit = 1u << 3;
 constexpr unsigned kFlagTensorBf16x3 = 1u << 4;
+constexpr unsigned kFlagUnevenPerJob = 1u << 5;
 
 constexpr int kErrInval = -1;
 constexpr int kErrNotInit = -2;
@@ -117,6 +118,7 @@ static void teardown_locked() {
   if (!g.init) return;
   cudaSetDevice(g.device);
   cudaDeviceSynchronize();
+  release_uneven_plans();
   g.ws.release();
   g.hfilt.release();
   for (auto &b : g.hio) b.release();
@@ -372,7 +374,16 @@ int bridge_conv_uneven_device(const UnevenJob *jobs, unsigned njobs, const void 
   std::lock_guard<std::recursive_mutex> lk(g.mu);
   int rc = ensure_init_locked();
   if (rc) return rc;
-  // One job at a time; the persistent work-queue launch replaces this loop.
+  if (!(flags & (kFlagUnevenPerJob | kFlagTensorSplit | kFlagTensorBf16x3 | kFlagFilterIsSpectrum))) {
+    std::string err;
+    unsigned *status = device_status_address();
+    if (!status) return cuda_fail(cudaErrorInvalidSymbol, "device status word");
+    rc = uneven_persistent(jobs, njobs, d_sig, d_filt, d_out, (flags & kFlagNormalize) != 0, g.tw512, status,
+                           (cudaStream_t)stream, err);
+    if (rc) set_err(err);
+    return rc;
+  }
+  // One job at a time (CONVGPU_UNEVEN_PER_JOB, the tensor-core path, or precomputed spectra).
   size_t need = 0;
   for (unsigned j = 0; j < njobs; ++j) need = std::max(need, workspace_bytes_for(jobs[j].n, 1, flags & ~kFlagPerSignalFilter));
   cudaError_t e = g.ws.ensure(need);

@@ -7,6 +7,9 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <string>
+
+#include "abi_bridge.h"
 
 namespace convgpu {
 
@@ -28,6 +31,17 @@ cudaError_t launch_axis_pass_tc(int n, int axis, int op, const float2 *src, floa
 
 // Selects the TMA-fed y / z pass kernels (default) or the register-gather kernels.
 void set_tma_enabled(bool on);
+
+// Device address of the status word (for kernels outside passes.cu).
+unsigned int *device_status_address();
+
+// Uneven batch through the persistent work-queue launch (persistent.cu). Plans (work
+// items, counters, spectrum workspace, CUDA graph) are cached per sequence of sizes.
+// Returns 0 or a CONVGPU_E* code with `err` set.
+int uneven_persistent(const struct UnevenJob *jobs, unsigned njobs, const void *d_sig, const void *d_filt,
+                      void *d_out, bool normalize, const float2 *tw512, unsigned *status, cudaStream_t stream,
+                      std::string &err);
+void release_uneven_plans();
 
 // Returns and clears the device status word (kStatus* bits; ~0 if it cannot be read).
 unsigned int read_and_clear_device_status();

@@ -197,6 +197,12 @@ static cudaError_t launch_tma_op(int axis, int op, PassArgs a, int nvol, cudaStr
 static bool g_use_tma = true;
 void set_tma_enabled(bool on) { g_use_tma = on; }
 
+unsigned int *device_status_address() {
+  void *p = nullptr;
+  if (cudaGetSymbolAddress(&p, g_device_status) != cudaSuccess) return nullptr;
+  return static_cast<unsigned int *>(p);
+}
+
 unsigned int read_and_clear_device_status() {
   unsigned int v = 0;
   if (cudaMemcpyFromSymbol(&v, g_device_status, sizeof(v)) != cudaSuccess) return ~0u;

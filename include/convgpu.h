@@ -25,6 +25,7 @@ extern "C" {
 #define CONVGPU_FILTER_IS_SPECTRUM (1u << 2)   /* filter already holds FFT3(filter) */
 #define CONVGPU_TENSOR_SPLIT (1u << 3)         /* tensor-core path, split TF32 (TF32x3) */
 #define CONVGPU_TENSOR_BF16X3 (1u << 4)        /* tensor-core path, BF16x3 split (implies TENSOR_SPLIT) */
+#define CONVGPU_UNEVEN_PER_JOB (1u << 5)       /* uneven batch: one job at a time, not the work queue */
 
 /* Status codes */
 #define CONVGPU_OK 0
@@ -86,7 +87,12 @@ typedef struct {
 } convgpu_job;
 
 /* Convolutions of different power-of-two sizes in one call (one filter per job),
- * on device pointers. Extends fpgaf_conv3D_svm_batch to uneven sizes. */
+ * on device pointers. Extends fpgaf_conv3D_svm_batch to uneven sizes.
+ * Default: one persistent launch fed by a device work queue of (job, pass, tile) items,
+ * replayed from a CUDA graph cached per sequence of sizes (at most 4096 jobs; the
+ * graph and the filter-spectrum workspace stay allocated until fpga_final). With
+ * CONVGPU_UNEVEN_PER_JOB, CONVGPU_TENSOR_SPLIT or CONVGPU_FILTER_IS_SPECTRUM the jobs
+ * run one after another through the per-size pass kernels instead. */
 int convgpu_conv3d_uneven_device(const convgpu_job *jobs, unsigned njobs, const float2 *d_sig_base,
                                  const float2 *d_filter_base, float2 *d_out_base, unsigned flags, void *stream);
 

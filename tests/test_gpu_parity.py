@@ -218,3 +218,57 @@ def test_unaligned_pointers_use_gather_kernels(gpu, n):
 def test_device_status_clean(gpu):
     """No kernel gave up a bounded wait during the tests above."""
     assert gpu.device_status() == 0
+
+
+def _uneven_inputs(sizes, seed):
+    rng = np.random.default_rng(seed)
+    sigs = [_c64(rng, (n, n, n)) for n in sizes]
+    filts = [gaussian_filter(n, float(rng.uniform(1.0, 8.0))) for n in sizes]
+    offs = np.cumsum([0] + [n ** 3 for n in sizes])
+    return sigs, filts, offs
+
+
+@pytest.mark.parametrize("mode", ["queue", "per_job"])
+def test_uneven_config_sizes_queue_and_replay(gpu, mode):
+    """The uneven workload's size mix (drawn from {32,64,128,256}), first 20 jobs; the
+    work-queue launch is replayed from its cached CUDA graph with new data."""
+    from oracle import uneven_sizes
+
+    sizes = uneven_sizes()[:20]
+    flags = gpu.NORMALIZE | (gpu.UNEVEN_PER_JOB if mode == "per_job" else 0)
+    for rep in range(2):
+        sigs, filts, offs = _uneven_inputs(sizes, 100 + rep)
+        s = torch.from_numpy(np.concatenate([x.ravel() for x in sigs])).cuda()
+        f = torch.from_numpy(np.concatenate([x.ravel() for x in filts])).cuda()
+        o = torch.empty_like(s)
+        jobs = [(n, int(offs[i]), int(offs[i]), int(offs[i])) for i, n in enumerate(sizes)]
+        gpu.conv3d_uneven_device(jobs, s, f, o, flags)
+        torch.cuda.synchronize()
+        oh = o.cpu().numpy()
+        for i, n in enumerate(sizes):
+            ref = conv3d(sigs[i], filts[i], "fp32", normalize=True, engine="pocketfft")
+            assert snr_db(ref, oh[offs[i]:offs[i + 1]].reshape(n, n, n)) > SNR_DB, (i, n)
+    assert gpu.device_status() == 0
+
+
+def test_uneven_in_place_and_distinct_offsets(gpu):
+    """Jobs whose signal, filter and output live at unrelated offsets, outputs in place."""
+    rng = np.random.default_rng(77)
+    sizes = [64, 32, 128, 64]
+    sigs, filts, offs = _uneven_inputs(sizes, 78)
+    total = int(offs[-1])
+    s = torch.from_numpy(np.concatenate([x.ravel() for x in sigs])).cuda()
+    f_perm = list(reversed(range(len(sizes))))
+    f_offs, pos = {}, 0
+    for i in f_perm:
+        f_offs[i] = pos
+        pos += sizes[i] ** 3
+    f = torch.from_numpy(np.concatenate([filts[i].ravel() for i in f_perm])).cuda()
+    jobs = [(n, int(offs[i]), f_offs[i], int(offs[i])) for i, n in enumerate(sizes)]
+    gpu.conv3d_uneven_device(jobs, s, f, s, 0)
+    torch.cuda.synchronize()
+    oh = s.cpu().numpy()
+    assert oh.size == total
+    for i, n in enumerate(sizes):
+        ref = conv3d(sigs[i], filts[i], "fp32", engine="pocketfft")
+        assert snr_db(ref, oh[offs[i]:offs[i + 1]].reshape(n, n, n)) > SNR_DB
