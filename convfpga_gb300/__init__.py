@@ -35,6 +35,7 @@ FILTER_IS_SPECTRUM = 1 << 2
 TENSOR_SPLIT = 1 << 3
 TENSOR_BF16X3 = 1 << 4
 UNEVEN_PER_JOB = 1 << 5
+UNEVEN_QUEUE = 1 << 6
 
 OK, EINVAL, ENOTINIT, ECUDA, ENOMEM, EUNSUPPORTED = 0, -1, -2, -3, -4, -5
 

@@ -40,6 +40,7 @@ constexpr unsigned kFlagFilterIsSpectrum = 1u << 2;
 constexpr unsigned kFlagTensorSplit = 1u << 3;
 constexpr unsigned kFlagTensorBf16x3 = 1u << 4;
 constexpr unsigned kFlagUnevenPerJob = 1u << 5;
+constexpr unsigned kFlagUnevenQueue = 1u << 6;
 
 constexpr int kErrInval = -1;
 constexpr int kErrNotInit = -2;
@@ -119,6 +120,7 @@ static void teardown_locked() {
   cudaSetDevice(g.device);
   cudaDeviceSynchronize();
   release_uneven_plans();
+  release_grouped_plans();
   g.ws.release();
   g.hfilt.release();
   for (auto &b : g.hio) b.release();
@@ -374,14 +376,22 @@ int bridge_conv_uneven_device(const UnevenJob *jobs, unsigned njobs, const void 
   std::lock_guard<std::recursive_mutex> lk(g.mu);
   int rc = ensure_init_locked();
   if (rc) return rc;
+  const bool normalize = (flags & kFlagNormalize) != 0;
   if (!(flags & (kFlagUnevenPerJob | kFlagTensorSplit | kFlagTensorBf16x3 | kFlagFilterIsSpectrum))) {
     std::string err;
-    unsigned *status = device_status_address();
-    if (!status) return cuda_fail(cudaErrorInvalidSymbol, "device status word");
-    rc = uneven_persistent(jobs, njobs, d_sig, d_filt, d_out, (flags & kFlagNormalize) != 0, g.tw512, status,
-                           (cudaStream_t)stream, err);
-    if (rc) set_err(err);
-    return rc;
+    if (flags & kFlagUnevenQueue) {
+      unsigned *status = device_status_address();
+      if (!status) return cuda_fail(cudaErrorInvalidSymbol, "device status word");
+      rc = uneven_persistent(jobs, njobs, d_sig, d_filt, d_out, normalize, g.tw512, status, (cudaStream_t)stream, err);
+      if (rc) set_err(err);
+      return rc;
+    }
+    rc = uneven_grouped(jobs, njobs, d_sig, d_filt, d_out, normalize, g.tw512, (cudaStream_t)stream, err);
+    if (rc != kErrUnsupported) {
+      if (rc) set_err(err);
+      return rc;
+    }
+    // unaligned cubes: one job at a time below
   }
   // One job at a time (CONVGPU_UNEVEN_PER_JOB, the tensor-core path, or precomputed spectra).
   size_t need = 0;

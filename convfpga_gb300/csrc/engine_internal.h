@@ -32,6 +32,23 @@ cudaError_t launch_axis_pass_tc(int n, int axis, int op, const float2 *src, floa
 // Selects the TMA-fed y / z pass kernels (default) or the register-gather kernels.
 void set_tma_enabled(bool on);
 
+// Table-mode launches (one launch over cubes at unrelated addresses): per-volume tensor
+// maps of the source (and, for the fused z pass, of the filter spectrum) and per-volume
+// destination bases, all in device memory. encode_table_map fills the map of one cube
+// for kind 0 (rows, x pass), 1 (y pass) or 2 (z pass) with the box of that size's kernel.
+#include <cuda.h>
+bool encode_table_map(CUtensorMap *m, const void *cube, int n, int kind);
+// Sets the kernel attributes the table-mode launches of size n need (call before a
+// stream capture that contains them).
+cudaError_t prepare_table_launches(int n);
+cudaError_t launch_axis_pass_table(int n, int axis, int op, const CUtensorMap *maps, const CUtensorMap *fmaps,
+                                   float2 *const *dsts, int nvol, float scale, const float2 *tw512,
+                                   cudaStream_t s);
+// Uneven batch as one CUDA graph of per-size table-mode launches (grouped.cu).
+int uneven_grouped(const struct UnevenJob *jobs, unsigned njobs, const void *d_sig, const void *d_filt,
+                   void *d_out, bool normalize, const float2 *tw512, cudaStream_t stream, std::string &err);
+void release_grouped_plans();
+
 // Device address of the status word (for kernels outside passes.cu).
 unsigned int *device_status_address();
 

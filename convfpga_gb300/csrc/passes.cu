@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <cstring>
 #include <mutex>
 
 #include "engine_internal.h"
@@ -273,6 +274,115 @@ cudaError_t launch_axis_pass(int n, int axis, int op, const float2 *src, float2 
     case 128: return launch_n<128>(axis, op, a, nvol, s);
     case 256: return launch_n<256>(axis, op, a, nvol, s);
     case 512: return launch_n<512>(axis, op, a, nvol, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+// ------------------------------------------------------------------ table mode
+bool encode_table_map(CUtensorMap *m, const void *cube, int n, int kind) {
+  auto go = [&](auto shape) {
+    using S = decltype(shape);
+    if (kind == 0) return encode_rows_map(m, cube, n, (long long)n * n, S::XC);
+    return encode_cube_map(m, cube, n, n, kind, S::SC);
+  };
+  switch (n) {
+    case 16: return go(Shape<16>{});
+    case 32: return go(Shape<32>{});
+    case 64: return go(Shape<64>{});
+    case 128: return go(Shape<128>{});
+    case 256: return go(Shape<256>{});
+    case 512: return go(Shape<512>{});
+    default: return false;
+  }
+}
+
+template <int N, int OP>
+static cudaError_t launch_table_n(int axis, PassArgs a, int nvol, cudaStream_t s) {
+  using S = Shape<N>;
+  constexpr int E = S::E;
+  CUtensorMap dummy;
+  std::memset(&dummy, 0, sizeof(dummy));
+  if (axis == 0) {
+    if constexpr (OP == OP_FWD || OP == OP_INV) {
+      constexpr int XC = S::XC;
+      constexpr int smem = tma_rows_smem_bytes<N, XC>();
+      auto kern = k_rows_tma<N, E, XC, OP, typename S::Plan>;  // attributes: prepare_table_launches
+      kern<<<(unsigned)((long long)nvol * N * N / XC), XC * (N / E), smem, s>>>(dummy, a);
+      return cudaGetLastError();
+    }
+    return cudaErrorInvalidValue;
+  }
+  constexpr int COLS = S::SC;
+  constexpr int smem = tma_pass_smem_bytes<N, COLS, OP>();
+  auto kern = k_strided_tma<N, E, COLS, OP, typename S::Plan>;  // attributes: prepare_table_launches
+  a.groups_x = N / COLS;
+  a.groups_per_vol = N * (N / COLS);
+  a.axis_stride = axis == 1 ? N : (long long)N * N;
+  a.plane_pitch = axis == 1 ? (long long)N * N : N;
+  kern<<<(unsigned)((long long)nvol * a.groups_per_vol), COLS * (N / E), smem, s>>>(dummy, dummy, a, axis);
+  return cudaGetLastError();
+}
+
+template <int N>
+static cudaError_t prepare_table_n() {
+  using S = Shape<N>;
+  constexpr int E = S::E, XC = S::XC, COLS = S::SC;
+  cudaError_t e = cudaSuccess;
+  auto set = [&](auto kern, int smem) {
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  };
+  set(k_rows_tma<N, E, XC, OP_FWD, typename S::Plan>, tma_rows_smem_bytes<N, XC>());
+  set(k_rows_tma<N, E, XC, OP_INV, typename S::Plan>, tma_rows_smem_bytes<N, XC>());
+  set(k_strided_tma<N, E, COLS, OP_FWD, typename S::Plan>, tma_pass_smem_bytes<N, COLS, OP_FWD>());
+  set(k_strided_tma<N, E, COLS, OP_INV, typename S::Plan>, tma_pass_smem_bytes<N, COLS, OP_INV>());
+  set(k_strided_tma<N, E, COLS, OP_CONV, typename S::Plan>, tma_pass_smem_bytes<N, COLS, OP_CONV>());
+  set(k_strided_tma<N, E, COLS, OP_CONV_FZ, typename S::Plan>, tma_pass_smem_bytes<N, COLS, OP_CONV_FZ>());
+  return e;
+}
+
+cudaError_t prepare_table_launches(int n) {
+  switch (n) {
+    case 16: return prepare_table_n<16>();
+    case 32: return prepare_table_n<32>();
+    case 64: return prepare_table_n<64>();
+    case 128: return prepare_table_n<128>();
+    case 256: return prepare_table_n<256>();
+    case 512: return prepare_table_n<512>();
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+template <int N>
+static cudaError_t launch_table_op(int axis, int op, PassArgs a, int nvol, cudaStream_t s) {
+  switch (op) {
+    case OP_FWD: return launch_table_n<N, OP_FWD>(axis, a, nvol, s);
+    case OP_INV: return launch_table_n<N, OP_INV>(axis, a, nvol, s);
+    case OP_CONV: return launch_table_n<N, OP_CONV>(axis, a, nvol, s);
+    case OP_CONV_FZ: return launch_table_n<N, OP_CONV_FZ>(axis, a, nvol, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t launch_axis_pass_table(int n, int axis, int op, const CUtensorMap *maps, const CUtensorMap *fmaps,
+                                   float2 *const *dsts, int nvol, float scale, const float2 *tw512,
+                                   cudaStream_t s) {
+  if (nvol <= 0) return cudaSuccess;
+  if ((op == OP_CONV || op == OP_CONV_FZ) && (axis != 2 || !fmaps)) return cudaErrorInvalidValue;
+  PassArgs a{};
+  a.tw512 = tw512;
+  a.scale = scale;
+  a.vol_elems = (long long)n * n * n;
+  a.filt_vol_elems = (long long)n * n * n;
+  a.maps = maps;
+  a.fmaps = fmaps;
+  a.dsts = dsts;
+  switch (n) {
+    case 16: return launch_table_op<16>(axis, op, a, nvol, s);
+    case 32: return launch_table_op<32>(axis, op, a, nvol, s);
+    case 64: return launch_table_op<64>(axis, op, a, nvol, s);
+    case 128: return launch_table_op<128>(axis, op, a, nvol, s);
+    case 256: return launch_table_op<256>(axis, op, a, nvol, s);
+    case 512: return launch_table_op<512>(axis, op, a, nvol, s);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -42,6 +42,12 @@ struct PassArgs {
   int groups_per_vol;      // CTAs per volume
   int groups_x;            // strided: N / COLS
   float scale;             // INV / CONV: output scale
+  // Table mode of the TMA kernels (null otherwise): per-volume tensor maps of the source
+  // and filter operands (each map covers one cube) and per-volume destination bases, so
+  // one launch serves cubes at unrelated addresses.
+  const CUtensorMap *maps;
+  const CUtensorMap *fmaps;
+  float2 *const *dsts;
 };
 
 // Shared-memory slot of pencil position n for the two layouts.
@@ -224,16 +230,21 @@ __global__ void __launch_bounds__(COLS *(N / E)) k_strided_tma(const __grid_cons
   }
   __syncthreads();
   if (threadIdx.x == 0) {
+    const CUtensorMap *ms = a.maps ? a.maps + vol : &msrc;
+    const int zoff = a.maps ? 0 : vol * N;
+    if (a.maps) tensormap_acquire(ms);
     mbar_arrive_expect_tx(bar, (HAS_F ? 2u : 1u) * TILE * 8u);
 #pragma unroll
     for (int l = 0; l < NLOADS; ++l) {
       if (axis == 1)
-        tma_load_3d(smem_u32(tile + l * NBOX * COLS), &msrc, x0, l * NBOX, vol * N + row, bar);
+        tma_load_3d(smem_u32(tile + l * NBOX * COLS), ms, x0, l * NBOX, zoff + row, bar);
       else
-        tma_load_3d(smem_u32(tile + l * NBOX * COLS), &msrc, x0, row, vol * N + l * NBOX, bar);
+        tma_load_3d(smem_u32(tile + l * NBOX * COLS), ms, x0, row, zoff + l * NBOX, bar);
       if constexpr (HAS_F) {
-        const int fv = a.filt_vol_elems ? vol : 0;
-        tma_load_3d(smem_u32(ftile + l * NBOX * COLS), &mfilt, x0, row, fv * N + l * NBOX, bar);
+        const CUtensorMap *mf = a.fmaps ? a.fmaps + vol : &mfilt;
+        const int fzoff = a.fmaps ? 0 : (a.filt_vol_elems ? vol : 0) * N;
+        if (a.fmaps && l == 0) tensormap_acquire(mf);
+        tma_load_3d(smem_u32(ftile + l * NBOX * COLS), mf, x0, row, fzoff + l * NBOX, bar);
       }
     }
   }
@@ -281,7 +292,7 @@ __global__ void __launch_bounds__(COLS *(N / E)) k_strided_tma(const __grid_cons
 #pragma unroll
     for (int e = 0; e < E; ++e) v[e] = make_float2(v[e].x * a.scale, v[e].y * a.scale);
   }
-  float2 *dst = a.dst + (long long)vol * a.vol_elems + (long long)row * a.plane_pitch + x0 + c;
+  float2 *dst = (a.dsts ? a.dsts[vol] : a.dst + (long long)vol * a.vol_elems) + (long long)row * a.plane_pitch + x0 + c;
 #pragma unroll
   for (int e = 0; e < E; ++e) dst[(long long)(t + e * T) * a.axis_stride] = v[e];
 }
@@ -301,7 +312,10 @@ __global__ void __launch_bounds__(XC *(N / E)) k_rows_tma(const __grid_constant_
   float2 *exch = tile + XC * N;
   float2 *tw = exch + XC * row_pitch<N>();
   const uint32_t bar = smem_u32(smraw);
-  const long long row0 = (long long)blockIdx.x * XC;
+  // Table mode: blockIdx -> (volume, row tile) and the volume's own map / destination.
+  constexpr int TPV = N * N / XC;
+  const int vol = a.maps ? (int)(blockIdx.x / TPV) : 0;
+  const long long row0 = a.maps ? (long long)(blockIdx.x % TPV) * XC : (long long)blockIdx.x * XC;
 
   if (threadIdx.x == 0) {
     mbar_init(bar, 1);
@@ -309,10 +323,12 @@ __global__ void __launch_bounds__(XC *(N / E)) k_rows_tma(const __grid_constant_
   }
   __syncthreads();
   if (threadIdx.x == 0) {
+    const CUtensorMap *ms = a.maps ? a.maps + vol : &msrc;
+    if (a.maps) tensormap_acquire(ms);
     mbar_arrive_expect_tx(bar, (uint32_t)(XC * N * 8));
 #pragma unroll
     for (int l = 0; l < NLOADS; ++l)
-      tma_load_2d(smem_u32(tile + l * XC * NBOX), &msrc, l * NBOX, (int)row0, bar);
+      tma_load_2d(smem_u32(tile + l * XC * NBOX), ms, l * NBOX, (int)row0, bar);
   }
   for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = a.tw512[i * (512 / N)];
   const int t = threadIdx.x % T;
@@ -334,7 +350,7 @@ __global__ void __launch_bounds__(XC *(N / E)) k_rows_tma(const __grid_constant_
 #pragma unroll
     for (int e = 0; e < E; ++e) v[e] = make_float2(v[e].x * a.scale, v[e].y * a.scale);
   }
-  float2 *dst = a.dst + (row0 + c) * N + t;
+  float2 *dst = (a.dsts ? a.dsts[vol] : a.dst) + (row0 + c) * N + t;
 #pragma unroll
   for (int e = 0; e < E; ++e) dst[e * T] = v[e];
 }

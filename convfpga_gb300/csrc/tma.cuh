@@ -53,6 +53,13 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity)
   return false;
 }
 
+// Orders the async proxy's view of a 128-byte tensor map held in global memory after the
+// generic writes that produced it (maps uploaded to device arrays).
+__device__ __forceinline__ void tensormap_acquire(const CUtensorMap *map) {
+  asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(reinterpret_cast<uint64_t>(map))
+               : "memory");
+}
+
 // 2D tiled load of the box at (c0, c1) (c0 innermost).
 __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int c0, int c1, uint32_t bar) {
   asm volatile(

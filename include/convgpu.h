@@ -25,7 +25,8 @@ extern "C" {
 #define CONVGPU_FILTER_IS_SPECTRUM (1u << 2)   /* filter already holds FFT3(filter) */
 #define CONVGPU_TENSOR_SPLIT (1u << 3)         /* tensor-core path, split TF32 (TF32x3) */
 #define CONVGPU_TENSOR_BF16X3 (1u << 4)        /* tensor-core path, BF16x3 split (implies TENSOR_SPLIT) */
-#define CONVGPU_UNEVEN_PER_JOB (1u << 5)       /* uneven batch: one job at a time, not the work queue */
+#define CONVGPU_UNEVEN_PER_JOB (1u << 5)       /* uneven batch: one job at a time */
+#define CONVGPU_UNEVEN_QUEUE (1u << 6)         /* uneven batch: one persistent work-queue launch */
 
 /* Status codes */
 #define CONVGPU_OK 0
@@ -88,11 +89,14 @@ typedef struct {
 
 /* Convolutions of different power-of-two sizes in one call (one filter per job),
  * on device pointers. Extends fpgaf_conv3D_svm_batch to uneven sizes.
- * Default: one persistent launch fed by a device work queue of (job, pass, tile) items,
- * replayed from a CUDA graph cached per sequence of sizes (at most 4096 jobs; the
- * graph and the filter-spectrum workspace stay allocated until fpga_final). With
- * CONVGPU_UNEVEN_PER_JOB, CONVGPU_TENSOR_SPLIT or CONVGPU_FILTER_IS_SPECTRUM the jobs
- * run one after another through the per-size pass kernels instead. */
+ * Default: one CUDA graph, cached per sequence of job sizes, in which every size class is
+ * a branch of seven launches (one per pass) over all jobs of that size; tensor maps are
+ * rebuilt only when a job's buffers move. CONVGPU_UNEVEN_QUEUE runs the batch as one
+ * persistent launch fed by a device work queue of (job, pass, tile) items (at most
+ * 4096 jobs), also replayed from a cached graph. Graphs and filter-spectrum workspaces
+ * stay allocated until fpga_final. With CONVGPU_UNEVEN_PER_JOB, CONVGPU_TENSOR_SPLIT,
+ * CONVGPU_FILTER_IS_SPECTRUM, or cubes not 16-byte aligned, the jobs run one after
+ * another through the per-size pass kernels. */
 int convgpu_conv3d_uneven_device(const convgpu_job *jobs, unsigned njobs, const float2 *d_sig_base,
                                  const float2 *d_filter_base, float2 *d_out_base, unsigned flags, void *stream);
 

@@ -228,14 +228,15 @@ def _uneven_inputs(sizes, seed):
     return sigs, filts, offs
 
 
-@pytest.mark.parametrize("mode", ["queue", "per_job"])
+@pytest.mark.parametrize("mode", ["grouped", "queue", "per_job"])
 def test_uneven_config_sizes_queue_and_replay(gpu, mode):
     """The uneven workload's size mix (drawn from {32,64,128,256}), first 20 jobs; the
-    work-queue launch is replayed from its cached CUDA graph with new data."""
+    grouped and work-queue launches are replayed from their cached CUDA graphs with new
+    data (new buffers, so the grouped plan re-encodes its tensor maps)."""
     from oracle import uneven_sizes
 
     sizes = uneven_sizes()[:20]
-    flags = gpu.NORMALIZE | (gpu.UNEVEN_PER_JOB if mode == "per_job" else 0)
+    flags = gpu.NORMALIZE | {"grouped": 0, "queue": gpu.UNEVEN_QUEUE, "per_job": gpu.UNEVEN_PER_JOB}[mode]
     for rep in range(2):
         sigs, filts, offs = _uneven_inputs(sizes, 100 + rep)
         s = torch.from_numpy(np.concatenate([x.ravel() for x in sigs])).cuda()
