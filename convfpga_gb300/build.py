@@ -20,6 +20,8 @@ CSRC = os.path.join(PKG, "csrc")
 INCLUDE = os.path.join(ROOT, "include")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libconvgpu.so")
+APP_SRC = os.path.join(PKG, "app", "convolution.cpp")
+APP = os.path.join(PKG, "convolution")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
@@ -88,7 +90,22 @@ def build(verbose: bool = False, force: bool = False) -> str:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed\n{r.stdout}\n{r.stderr}")
+    build_app(verbose)
     return LIB
+
+
+def build_app(verbose: bool = False) -> str:
+    """The `convolution` sample application, linked against libconvgpu.so (rpath $ORIGIN)."""
+    if os.path.exists(APP) and os.path.getmtime(APP) >= max(os.path.getmtime(APP_SRC), os.path.getmtime(LIB)):
+        return APP
+    cmd = [os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-Wall", "-I", INCLUDE, APP_SRC, "-o", APP,
+           "-L", PKG, "-lconvgpu", "-Wl,-rpath,$ORIGIN", "-lpthread"]
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"app build failed\n{r.stdout}\n{r.stderr}")
+    return APP
 
 
 if __name__ == "__main__":
