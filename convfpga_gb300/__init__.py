@@ -60,6 +60,8 @@ EXPORTED_SYMBOLS = (
     "convgpu_pass_timing",
     "convgpu_synchronize",
     "convgpu_device_status",
+    "convgpu_autotune",
+    "convgpu_plan_variant",
     "convgpu_last_error",
 )
 
@@ -147,6 +149,10 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
     lib.convgpu_synchronize.restype = ctypes.c_int
     lib.convgpu_device_status.argtypes = [ctypes.POINTER(ctypes.c_uint)]
     lib.convgpu_device_status.restype = ctypes.c_int
+    lib.convgpu_autotune.argtypes = [ctypes.POINTER(ctypes.c_uint), ctypes.c_uint, ctypes.c_int]
+    lib.convgpu_autotune.restype = ctypes.c_int
+    lib.convgpu_plan_variant.argtypes = [ctypes.c_uint, ctypes.c_int, ctypes.c_int]
+    lib.convgpu_plan_variant.restype = ctypes.c_int
     lib.convgpu_last_error.argtypes = []
     lib.convgpu_last_error.restype = ctypes.c_char_p
     if path is None:
@@ -295,6 +301,22 @@ def pass_timing_read() -> dict:
         if cnt[i]:
             out[f"{PASS_AXES[i // 4]}-{PASS_OPS[i % 4]}"] = {"ms": ms[i], "launches": int(cnt[i]), "bytes": by[i]}
     return out
+
+
+PLAN_KINDS = ("rows", "strided", "conv", "conv_fz")
+
+
+def autotune(sizes, write_cache: bool = True) -> None:
+    """Times both shape variants per pass kind for each size and keeps the faster."""
+    arr = (ctypes.c_uint * len(sizes))(*sizes)
+    _check(load_library().convgpu_autotune(arr, len(sizes), 1 if write_cache else 0), "convgpu_autotune")
+
+
+def plan_variant(n: int, kind: int, set_to: int = -1) -> int:
+    v = load_library().convgpu_plan_variant(n, kind, set_to)
+    if v < 0:
+        raise ConvGpuError(f"convgpu_plan_variant failed ({v}): {last_error()}")
+    return v
 
 
 def device_status() -> int:

@@ -44,6 +44,8 @@ const char *bridge_last_error();
 int bridge_host_alloc_pinned(size_t bytes, void **ptr);
 int bridge_host_free_pinned(void *ptr);
 int bridge_sync();
+int bridge_autotune(const unsigned *sizes, unsigned count, int write_cache);
+int bridge_plan_variant(unsigned n, int kind, int set_to);
 int bridge_device_status(unsigned *status);
 
 }  // namespace convgpu

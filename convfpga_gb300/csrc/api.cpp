@@ -98,6 +98,12 @@ int convgpu_pass_timing(int mode, double *ms, unsigned long long *launches, doub
 
 int convgpu_synchronize(void) { return convgpu::bridge_sync(); }
 
+int convgpu_autotune(const unsigned *sizes, unsigned count, int write_cache) {
+  return convgpu::bridge_autotune(sizes, count, write_cache);
+}
+
+int convgpu_plan_variant(unsigned N, int kind, int set_to) { return convgpu::bridge_plan_variant(N, kind, set_to); }
+
 int convgpu_device_status(unsigned *status) { return convgpu::bridge_device_status(status); }
 
 const char *convgpu_last_error(void) { return convgpu::bridge_last_error(); }

@@ -102,6 +102,7 @@ struct Engine {
   std::string plan_path;
 };
 static Engine g;
+static void load_plan_cache(const std::string &path);
 
 static cudaError_t upload_twiddles(float2 **dst) {
   std::vector<float2> h(512);
@@ -315,7 +316,9 @@ int bridge_initialize(const char *platform_name, const char *path, bool use_svm)
     }
   }
   g.plan_path = path;
-  return setup_locked(dev, use_svm);
+  const int rc = setup_locked(dev, use_svm);
+  if (rc == 0) load_plan_cache(g.plan_path);  // anything that is not a plan cache is ignored
+  return rc;
 }
 
 void bridge_final() {
@@ -563,6 +566,133 @@ Timing bridge_conv_host(unsigned n, const void *sig, const void *filt, void *out
   }
   t.valid = true;
   return t;
+}
+
+// ------------------------------------------------------------------ autotuner / plan cache
+// The plan cache plays the role of the reference CPU path's FFTW wisdom file
+// (src/fft_conv3D.cpp:85-112): one line per cube size with the shape variant chosen for
+// each pass kind and the timings (microseconds per launch, variants 0 and 1) it was
+// chosen from.
+static const char *kKindNames[kPassKinds] = {"rows", "strided", "conv", "conv_fz"};
+
+static void load_plan_cache(const std::string &path) {
+  FILE *f = std::fopen(path.c_str(), "r");
+  if (!f) return;
+  char line[1024];
+  while (std::fgets(line, sizeof(line), f)) {
+    int n = 0;
+    const char *q = std::strchr(line, '"');
+    if (!q || std::sscanf(q, "\"%d\": {", &n) != 1 || !valid_n((unsigned)n)) continue;
+    for (int k = 0; k < kPassKinds; ++k) {
+      const std::string key = std::string("\"") + kKindNames[k] + "\": ";
+      const char *p = std::strstr(line, key.c_str());
+      int v = 0;
+      if (p && std::sscanf(p + key.size(), "%d", &v) == 1) set_pass_variant(n, k, v);
+    }
+  }
+  std::fclose(f);
+}
+
+struct TuneRow {
+  int n;
+  int choice[kPassKinds];
+  double us[2][kPassKinds];
+};
+static std::vector<TuneRow> g_tuned;
+
+static bool write_plan_cache(const std::string &path) {
+  FILE *f = std::fopen(path.c_str(), "w");
+  if (!f) return false;
+  cudaDeviceProp prop{};
+  cudaGetDeviceProperties(&prop, g.device);
+  std::fprintf(f, "{\"convgpu_plan_cache\": 1, \"device\": \"%s\", \"sizes\": {\n", prop.name);
+  for (size_t i = 0; i < g_tuned.size(); ++i) {
+    const TuneRow &r = g_tuned[i];
+    std::fprintf(f, "  \"%d\": {", r.n);
+    for (int k = 0; k < kPassKinds; ++k) std::fprintf(f, "\"%s\": %d, ", kKindNames[k], r.choice[k]);
+    for (int v = 0; v < 2; ++v) {
+      std::fprintf(f, "\"us_v%d\": [", v);
+      for (int k = 0; k < kPassKinds; ++k) std::fprintf(f, "%.2f%s", r.us[v][k], k + 1 < kPassKinds ? ", " : "");
+      std::fprintf(f, "]%s", v == 0 ? ", " : "");
+    }
+    std::fprintf(f, "}%s\n", i + 1 < g_tuned.size() ? "," : "");
+  }
+  std::fprintf(f, "}}\n");
+  std::fclose(f);
+  return true;
+}
+
+// Times both shape variants of every pass kind for each size on a working set larger
+// than L2 and keeps the faster; optionally writes the plan cache.
+int bridge_autotune(const unsigned *sizes, unsigned count, int write_cache) {
+  if (!sizes && count) return kErrInval;
+  for (unsigned i = 0; i < count; ++i)
+    if (!valid_n(sizes[i])) {
+      set_err("autotune: unsupported size");
+      return kErrInval;
+    }
+  std::lock_guard<std::recursive_mutex> lk(g.mu);
+  int rc = ensure_init_locked();
+  if (rc) return rc;
+  cudaStream_t s = g.sc;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaError_t err = cudaSuccess;
+  for (unsigned i = 0; i < count && err == cudaSuccess; ++i) {
+    const int n = (int)sizes[i];
+    const size_t V = (size_t)n * n * n;
+    const int nvol = (int)std::max<size_t>(1, (size_t(256) << 20) / (V * sizeof(float2)));
+    err = g.ws.ensure(2 * nvol * V * sizeof(float2));
+    if (err != cudaSuccess) break;
+    float2 *data = (float2 *)g.ws.p;
+    float2 *spec = data + nvol * V;
+    cudaMemsetAsync(g.ws.p, 0, 2 * nvol * V * sizeof(float2), s);
+    TuneRow row{};
+    row.n = n;
+    for (int k = 0; k < kPassKinds && err == cudaSuccess; ++k) {
+      const int axis = k == kKindRows ? 0 : (k == kKindStrided ? 1 : 2);
+      const int op = k == kKindConv ? OP_CONV : (k == kKindConvFz ? OP_CONV_FZ : OP_FWD);
+      const long long fv = k == kKindConvFz ? (long long)V : 0;
+      for (int v = 0; v < 2 && err == cudaSuccess; ++v) {
+        auto run = [&]() {
+          return launch_axis_pass_variant(n, axis, op, data, data, spec, fv, nvol, 1.f, g.tw512, s, v);
+        };
+        for (int w = 0; w < 2 && err == cudaSuccess; ++w) err = run();
+        cudaEventRecord(e0, s);
+        for (int t = 0; t < 5 && err == cudaSuccess; ++t) err = run();
+        cudaEventRecord(e1, s);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        row.us[v][k] = 1000.0 * ms / 5.0;
+        count_launches(7);
+      }
+      row.choice[k] = row.us[1][k] < row.us[0][k] ? 1 : 0;
+      set_pass_variant(n, k, row.choice[k]);
+    }
+    g_tuned.erase(std::remove_if(g_tuned.begin(), g_tuned.end(), [&](const TuneRow &t) { return t.n == n; }),
+                  g_tuned.end());
+    g_tuned.push_back(row);
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (err != cudaSuccess) return cuda_fail(err, "autotune");
+  if (const unsigned st = read_and_clear_device_status()) {
+    set_err("autotune: device status " + std::to_string(st));
+    return kErrCuda;
+  }
+  if (write_cache && !g.plan_path.empty() && !write_plan_cache(g.plan_path)) {
+    set_err("autotune: cannot write the plan cache " + g.plan_path);
+    return kErrInval;
+  }
+  return 0;
+}
+
+int bridge_plan_variant(unsigned n, int kind, int set_to) {
+  if (!valid_n(n) || kind < 0 || kind >= kPassKinds) return kErrInval;
+  if (set_to >= 0) set_pass_variant((int)n, kind, set_to);
+  return get_pass_variant((int)n, kind);
 }
 
 // ------------------------------------------------------------------ bridge: misc

@@ -32,6 +32,17 @@ cudaError_t launch_axis_pass_tc(int n, int axis, int op, const float2 *src, floa
 // Selects the TMA-fed y / z pass kernels (default) or the register-gather kernels.
 void set_tma_enabled(bool on);
 
+// Plan table: shape variant (0 / 1) per cube size and pass kind, chosen by the
+// autotuner and recorded in the plan cache.
+constexpr int kKindRows = 0, kKindStrided = 1, kKindConv = 2, kKindConvFz = 3, kPassKinds = 4;
+int pass_kind(int axis, int op);
+void set_pass_variant(int n, int kind, int variant);
+int get_pass_variant(int n, int kind);
+// launch_axis_pass with an explicit shape variant (the autotuner times both).
+cudaError_t launch_axis_pass_variant(int n, int axis, int op, const float2 *src, float2 *dst, const float2 *filt,
+                                     long long filt_vol_elems, int nvol, float scale, const float2 *tw512,
+                                     cudaStream_t s, int variant);
+
 // Table-mode launches (one launch over cubes at unrelated addresses): per-volume tensor
 // maps of the source (and, for the fused z pass, of the filter spectrum) and per-volume
 // destination bases, all in device memory. encode_table_map fills the map of one cube

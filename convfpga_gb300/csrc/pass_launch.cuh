@@ -1,0 +1,220 @@
+// Launchers of the per-axis pass kernels for one cube size N, templated on N and
+// instantiated once per size in passes_n<N>.cu (so the sizes compile in parallel).
+//
+// Each size has two shape variants (radix list, elements per thread, pencils / rows per
+// CTA); a run-time plan table (set by the autotuner, recorded in the plan cache) picks
+// one per pass kind. The shapes replace the reference's synthesis-time FFT size and
+// fixed 8-points-per-cycle engine (kernels/common/conv_config.h.in:8-11).
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstring>
+
+#include "passes.cuh"
+
+namespace convgpu {
+
+// E: elements per thread; XC: rows per CTA (x pass); SC: columns per CTA (y / z passes).
+template <int N, int V>
+struct Shape;
+template <> struct Shape<16, 0> { static constexpr int E = 4, XC = 32, SC = 16; using Plan = Radices<4, 4>; };
+template <> struct Shape<16, 1> { static constexpr int E = 4, XC = 64, SC = 16; using Plan = Radices<4, 4>; };
+template <> struct Shape<32, 0> { static constexpr int E = 8, XC = 32, SC = 32; using Plan = Radices<8, 4>; };
+template <> struct Shape<32, 1> { static constexpr int E = 8, XC = 16, SC = 16; using Plan = Radices<4, 8>; };
+template <> struct Shape<64, 0> { static constexpr int E = 8, XC = 16, SC = 32; using Plan = Radices<8, 8>; };
+template <> struct Shape<64, 1> { static constexpr int E = 16, XC = 16, SC = 16; using Plan = Radices<16, 4>; };
+template <> struct Shape<128, 0> { static constexpr int E = 16, XC = 16, SC = 32; using Plan = Radices<16, 8>; };
+template <> struct Shape<128, 1> { static constexpr int E = 16, XC = 8, SC = 16; using Plan = Radices<8, 16>; };
+template <> struct Shape<256, 0> { static constexpr int E = 16, XC = 8, SC = 16; using Plan = Radices<16, 16>; };
+template <> struct Shape<256, 1> { static constexpr int E = 16, XC = 16, SC = 32; using Plan = Radices<16, 16>; };
+template <> struct Shape<512, 0> { static constexpr int E = 16, XC = 4, SC = 16; using Plan = Radices<16, 16, 2>; };
+template <> struct Shape<512, 1> { static constexpr int E = 8, XC = 2, SC = 16; using Plan = Radices<8, 8, 8>; };
+
+// One pass launch request.
+struct PassReq {
+  int mode;     // kModeTma (TMA kernels, register-gather kernels if maps are impossible),
+                // kModeTable (table-mode TMA), kModeGather (register-gather kernels)
+  int axis;     // 0 x, 1 y, 2 z
+  int op;       // OP_FWD, OP_INV, OP_CONV, OP_CONV_FZ
+  int nvol;
+  int variant;  // shape variant 0 / 1
+  PassArgs a;
+  cudaStream_t s;
+};
+constexpr int kModeTma = 0, kModeTable = 1, kModeGather = 2;
+
+// Tensor-map encoders (passes.cu). Return false when the operand cannot be described.
+bool encode_cube_map(CUtensorMap *m, const void *base, int n, long long nplanes, int axis, int cols);
+bool encode_rows_map(CUtensorMap *m, const void *base, int n, long long rows, int xc);
+
+template <int N>
+cudaError_t launch_size(const PassReq &r);
+template <int N>
+cudaError_t prepare_size();
+
+#ifdef CONVGPU_PASS_LAUNCH_IMPL
+
+template <class K>
+static cudaError_t set_smem_once(K kern, int smem, bool &done) {
+  if (done) return cudaSuccess;
+  const cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e == cudaSuccess) done = true;
+  return e;
+}
+
+// Register-gather kernels (shape variant 0): any 8-byte aligned operands.
+template <int N, bool CONTIG, int OP>
+static cudaError_t launch_gather(PassArgs a, int nvol, cudaStream_t s) {
+  using S = Shape<N, 0>;
+  constexpr int E = S::E;
+  constexpr int COLS = CONTIG ? S::XC : S::SC;
+  constexpr int smem = pass_smem_bytes<N, E, COLS, CONTIG>();
+  auto kern = k_axis_pass<N, E, COLS, CONTIG, OP, typename S::Plan>;
+  static bool done = false;
+  cudaError_t e = set_smem_once(kern, smem, done);
+  if (e != cudaSuccess) return e;
+  a.groups_x = N / S::SC;
+  a.groups_per_vol = N * (N / S::SC);
+  const long long blocks = CONTIG ? (long long)nvol * N * N / COLS : (long long)nvol * a.groups_per_vol;
+  if (blocks <= 0 || blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+  kern<<<(unsigned)blocks, COLS * (N / E), smem, s>>>(a);
+  return cudaGetLastError();
+}
+
+// TMA x pass. Returns cudaErrorNotSupported when a tensor map cannot be built.
+template <int N, int V, int OP>
+static cudaError_t launch_rows(const PassReq &r) {
+  using S = Shape<N, V>;
+  constexpr int E = S::E, XC = S::XC;
+  constexpr int smem = tma_rows_smem_bytes<N, XC>();
+  auto kern = k_rows_tma<N, E, XC, OP, typename S::Plan>;
+  static bool done = false;
+  cudaError_t e = set_smem_once(kern, smem, done);
+  if (e != cudaSuccess) return e;
+  CUtensorMap m;
+  std::memset(&m, 0, sizeof(m));
+  if (r.mode != kModeTable) {
+    if ((reinterpret_cast<uintptr_t>(r.a.dst) & 15u) != 0) return cudaErrorNotSupported;
+    if (!encode_rows_map(&m, r.a.src, N, (long long)r.nvol * N * N, XC)) return cudaErrorNotSupported;
+  }
+  const long long blocks = (long long)r.nvol * N * N / XC;
+  if (blocks <= 0 || blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+  kern<<<(unsigned)blocks, XC * (N / E), smem, r.s>>>(m, r.a);
+  return cudaGetLastError();
+}
+
+// TMA y / z pass. Returns cudaErrorNotSupported when a tensor map cannot be built.
+template <int N, int V, int OP>
+static cudaError_t launch_strided(const PassReq &r) {
+  using S = Shape<N, V>;
+  constexpr int E = S::E, COLS = S::SC;
+  constexpr bool HAS_F = (OP == OP_CONV || OP == OP_CONV_FZ);
+  constexpr int smem = tma_pass_smem_bytes<N, COLS, OP>();
+  auto kern = k_strided_tma<N, E, COLS, OP, typename S::Plan>;
+  static bool done = false;
+  cudaError_t e = set_smem_once(kern, smem, done);
+  if (e != cudaSuccess) return e;
+  PassArgs a = r.a;
+  a.groups_x = N / COLS;
+  a.groups_per_vol = N * (N / COLS);
+  a.axis_stride = r.axis == 1 ? N : (long long)N * N;
+  a.plane_pitch = r.axis == 1 ? (long long)N * N : N;
+  CUtensorMap msrc, mfilt;
+  std::memset(&msrc, 0, sizeof(msrc));
+  std::memset(&mfilt, 0, sizeof(mfilt));
+  if (r.mode != kModeTable) {
+    if ((reinterpret_cast<uintptr_t>(a.dst) & 15u) != 0) return cudaErrorNotSupported;
+    if (!encode_cube_map(&msrc, a.src, N, (long long)r.nvol * N, r.axis, COLS)) return cudaErrorNotSupported;
+    if (HAS_F) {
+      const long long fplanes = a.filt_vol_elems ? (long long)r.nvol * N : (long long)N;
+      if (!encode_cube_map(&mfilt, a.filt, N, fplanes, r.axis, COLS)) return cudaErrorNotSupported;
+    }
+  }
+  const long long blocks = (long long)r.nvol * a.groups_per_vol;
+  if (blocks <= 0 || blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+  kern<<<(unsigned)blocks, COLS * (N / E), smem, r.s>>>(msrc, mfilt, a, r.axis);
+  return cudaGetLastError();
+}
+
+template <int N, int V>
+static cudaError_t launch_tma_variant(const PassReq &r) {
+  if (r.axis == 0) {
+    if (r.op == OP_FWD) return launch_rows<N, V, OP_FWD>(r);
+    if (r.op == OP_INV) return launch_rows<N, V, OP_INV>(r);
+    return cudaErrorInvalidValue;
+  }
+  switch (r.op) {
+    case OP_FWD: return launch_strided<N, V, OP_FWD>(r);
+    case OP_INV: return launch_strided<N, V, OP_INV>(r);
+    case OP_CONV: return launch_strided<N, V, OP_CONV>(r);
+    case OP_CONV_FZ: return launch_strided<N, V, OP_CONV_FZ>(r);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+template <int N>
+static cudaError_t launch_gather_op(const PassReq &r) {
+  PassArgs a = r.a;
+  a.vol_elems = (long long)N * N * N;
+  if (r.axis == 0) {
+    if (r.op == OP_FWD) return launch_gather<N, true, OP_FWD>(a, r.nvol, r.s);
+    if (r.op == OP_INV) return launch_gather<N, true, OP_INV>(a, r.nvol, r.s);
+    return cudaErrorInvalidValue;
+  }
+  a.axis_stride = r.axis == 1 ? N : (long long)N * N;
+  a.plane_pitch = r.axis == 1 ? (long long)N * N : N;
+  switch (r.op) {
+    case OP_FWD: return launch_gather<N, false, OP_FWD>(a, r.nvol, r.s);
+    case OP_INV: return launch_gather<N, false, OP_INV>(a, r.nvol, r.s);
+    case OP_CONV: return launch_gather<N, false, OP_CONV>(a, r.nvol, r.s);
+    case OP_CONV_FZ: return launch_gather<N, false, OP_CONV_FZ>(a, r.nvol, r.s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+template <int N>
+cudaError_t launch_size(const PassReq &r) {
+  if (r.mode == kModeGather) return launch_gather_op<N>(r);
+  if (r.mode == kModeTable) return launch_tma_variant<N, 0>(r);  // tables are encoded with variant 0
+  const cudaError_t e = r.variant ? launch_tma_variant<N, 1>(r) : launch_tma_variant<N, 0>(r);
+  if (e != cudaErrorNotSupported) return e;
+  return launch_gather_op<N>(r);
+}
+
+template <int N, int V>
+static cudaError_t prepare_variant() {
+  using S = Shape<N, V>;
+  constexpr int E = S::E, XC = S::XC, COLS = S::SC;
+  cudaError_t e = cudaSuccess;
+  auto set = [&](auto kern, int smem) {
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  };
+  set(k_rows_tma<N, E, XC, OP_FWD, typename S::Plan>, tma_rows_smem_bytes<N, XC>());
+  set(k_rows_tma<N, E, XC, OP_INV, typename S::Plan>, tma_rows_smem_bytes<N, XC>());
+  set(k_strided_tma<N, E, COLS, OP_FWD, typename S::Plan>, tma_pass_smem_bytes<N, COLS, OP_FWD>());
+  set(k_strided_tma<N, E, COLS, OP_INV, typename S::Plan>, tma_pass_smem_bytes<N, COLS, OP_INV>());
+  set(k_strided_tma<N, E, COLS, OP_CONV, typename S::Plan>, tma_pass_smem_bytes<N, COLS, OP_CONV>());
+  set(k_strided_tma<N, E, COLS, OP_CONV_FZ, typename S::Plan>, tma_pass_smem_bytes<N, COLS, OP_CONV_FZ>());
+  return e;
+}
+
+// Sets the shared-memory attributes of every TMA kernel of size N (both variants), so
+// launches can later be captured into graphs.
+template <int N>
+cudaError_t prepare_size() {
+  cudaError_t e = prepare_variant<N, 0>();
+  if (e == cudaSuccess) e = prepare_variant<N, 1>();
+  return e;
+}
+
+#endif  // CONVGPU_PASS_LAUNCH_IMPL
+
+}  // namespace convgpu
+
+namespace convgpu {
+// Tensor-core pass for N = 256 (passes_n256.cu); bf16x3 selects BF16x3 over TF32x3.
+cudaError_t launch_tc256_entry(const PassReq &r, int bf16x3);
+}  // namespace convgpu

@@ -48,6 +48,8 @@ struct PassArgs {
   const CUtensorMap *maps;
   const CUtensorMap *fmaps;
   float2 *const *dsts;
+  // Device status word: kernels OR in kStatus* bits when a bounded wait gives up.
+  unsigned int *status;
 };
 
 // Shared-memory slot of pencil position n for the two layouts.
@@ -170,11 +172,6 @@ __global__ void __launch_bounds__(COLS *(N / E)) k_axis_pass(PassArgs a) {
   for (int e = 0; e < E; ++e) a.dst[base + (long long)(t + e * T) * es] = v[e];
 }
 
-// Device status word: kernels OR in kStatus* bits when a bounded wait gives up. Only
-// passes.cu instantiates kernels and reads it back; other translation units that include
-// this header never touch their copy.
-static __device__ unsigned int g_device_status;
-
 // Dynamic shared memory of the TMA-fed x pass: barrier slot, the unpadded row tile (TMA
 // target), the padded exchange buffer, then N twiddles.
 template <int N, int XC>
@@ -255,7 +252,7 @@ __global__ void __launch_bounds__(COLS *(N / E)) k_strided_tma(const __grid_cons
   // Uniform decision: every thread takes the same branch, so no barrier is left waiting.
   const int ok = __syncthreads_and(mbar_wait_bounded(bar, 0) ? 1 : 0);
   if (!ok) {
-    if (threadIdx.x == 0) atomicOr(&g_device_status, kStatusTmaTimeout);
+    if (threadIdx.x == 0 && a.status) atomicOr(a.status, kStatusTmaTimeout);
     mbar_wait_bounded(bar, 0);  // let copies still in flight land before the CTA exits
     return;
   }
@@ -336,7 +333,7 @@ __global__ void __launch_bounds__(XC *(N / E)) k_rows_tma(const __grid_constant_
   const RowSlot<N> sidx{c * row_pitch<N>()};
   const int ok = __syncthreads_and(mbar_wait_bounded(bar, 0) ? 1 : 0);
   if (!ok) {
-    if (threadIdx.x == 0) atomicOr(&g_device_status, kStatusTmaTimeout);
+    if (threadIdx.x == 0 && a.status) atomicOr(a.status, kStatusTmaTimeout);
     mbar_wait_bounded(bar, 0);
     return;
   }

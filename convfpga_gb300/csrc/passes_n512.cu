@@ -1,0 +1,8 @@
+// Pass-kernel launchers for cubes of size 512 (see pass_launch.cuh).
+#define CONVGPU_PASS_LAUNCH_IMPL
+#include "pass_launch.cuh"
+
+namespace convgpu {
+template cudaError_t launch_size<512>(const PassReq &);
+template cudaError_t prepare_size<512>();
+}  // namespace convgpu

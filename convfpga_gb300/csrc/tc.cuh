@@ -293,7 +293,7 @@ __global__ void __launch_bounds__(256) k_strided_tma_tc256(const __grid_constant
   for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = a.tw512[i * 2];
   const int ok = __syncthreads_and(mbar_wait_bounded(bar, 0) ? 1 : 0);
   if (!ok) {
-    if (threadIdx.x == 0) atomicOr(&g_device_status, kStatusTmaTimeout);
+    if (threadIdx.x == 0 && a.status) atomicOr(a.status, kStatusTmaTimeout);
     mbar_wait_bounded(bar, 0);
     return;
   }
@@ -371,7 +371,7 @@ __global__ void __launch_bounds__(256) k_rows_tma_tc256(const __grid_constant__ 
   for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = a.tw512[i * 2];
   const int ok = __syncthreads_and(mbar_wait_bounded(bar, 0) ? 1 : 0);
   if (!ok) {
-    if (threadIdx.x == 0) atomicOr(&g_device_status, kStatusTmaTimeout);
+    if (threadIdx.x == 0 && a.status) atomicOr(a.status, kStatusTmaTimeout);
     mbar_wait_bounded(bar, 0);
     return;
   }

@@ -129,6 +129,19 @@ int convgpu_pass_timing(int mode, double *ms, unsigned long long *launches, doub
 /* Waits for all work on the library's device. */
 int convgpu_synchronize(void);
 
+/* Autotuner: for each of `count` cube sizes, times both shape variants (radix split,
+ * pencils per CTA, rows per CTA) of every pass kind on a working set larger than L2 and
+ * keeps the faster. With write_cache, writes the choices and timings to the plan-cache
+ * file named by fpga_initialize's `path`; fpga_initialize reads that file back. The
+ * plan cache takes the role of the reference CPU path's FFTW wisdom file
+ * (src/fft_conv3D.cpp:85-112). Not safe to call while other calls are in flight. */
+int convgpu_autotune(const unsigned *sizes, unsigned count, int write_cache);
+
+/* Plan-table entry of cube size N for pass kind (0 x pass, 1 y/z passes, 2 fused z pass,
+ * 3 fused z pass with the filter's z transform): sets it to set_to (0 or 1) when
+ * set_to >= 0, and returns the current variant (or a negative CONVGPU_E* code). */
+int convgpu_plan_variant(unsigned N, int kind, int set_to);
+
 /* Waits for the device, then returns and clears the library's device status word in
  * *status: 0 when every kernel completed normally; bit 0 set when a kernel gave up a
  * bounded wait for its tile load (it then wrote no output for that tile). */

@@ -1,0 +1,91 @@
+"""Shape variants and the autotuner's plan cache (convgpu_autotune / convgpu_plan_variant).
+
+Every cube size has two shape variants (radix split, pencils per CTA, rows per CTA);
+both must give the oracle's results (SNR > 120 dB, the reference's criterion). The
+autotuner's choices survive a save / fpga_final / fpga_initialize round trip.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import conv3d, snr_db
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+KINDS = 4
+
+
+def _c64(rng, shape):
+    a = np.empty(shape, np.complex64)
+    a.real = rng.uniform(-1, 1, shape)
+    a.imag = rng.uniform(-1, 1, shape)
+    return a
+
+
+@pytest.fixture
+def restore_plans(gpu):
+    yield
+    for n in (16, 32, 64, 128, 256, 512):
+        for k in range(KINDS):
+            gpu.plan_variant(n, k, 0)
+
+
+def _check(gpu, n, b, per_signal):
+    rng = np.random.default_rng(n * 3 + per_signal)
+    sig = _c64(rng, (b, n, n, n))
+    filt = _c64(rng, (b, n, n, n)) if per_signal else _c64(rng, (n, n, n))
+    s = torch.from_numpy(sig).cuda()
+    f = torch.from_numpy(filt).cuda()
+    o = torch.empty_like(s)
+    gpu.conv3d_device(n, s, f, o, b, gpu.FILTER_PER_SIGNAL if per_signal else 0)
+    torch.cuda.synchronize()
+    ref = conv3d(sig, filt, "fp32", engine="pocketfft")
+    assert snr_db(ref, o.cpu().numpy()) > 120.0
+
+
+@pytest.mark.parametrize("n", [16, 32, 64, 128, 256])
+@pytest.mark.parametrize("variant", [0, 1])
+def test_every_variant_matches_the_oracle(gpu, restore_plans, n, variant):
+    for k in range(KINDS):
+        assert gpu.plan_variant(n, k, variant) == variant
+    b = 2 if n <= 128 else 1
+    _check(gpu, n, b, per_signal=False)  # x, y/z and fused z (CONV) kernels
+    _check(gpu, n, b, per_signal=True)   # fused z with the filter's z transform (CONV_FZ)
+    assert gpu.device_status() == 0
+
+
+@pytest.mark.slow
+@pytest.mark.parametrize("variant", [0, 1])
+def test_512_variants(gpu, restore_plans, variant):
+    for k in range(KINDS):
+        gpu.plan_variant(512, k, variant)
+    _check(gpu, 512, 1, per_signal=True)
+
+
+def test_autotune_plan_cache_round_trip(gpu, restore_plans, tmp_path):
+    path = str(tmp_path / "plans.json")
+    gpu.fpga_final()
+    assert gpu.fpga_initialize("cuda:0", path, False) == 0
+    gpu.autotune([32, 128, 256], write_cache=True)
+    chosen = {n: [gpu.plan_variant(n, k) for k in range(KINDS)] for n in (32, 128, 256)}
+    text = open(path).read()
+    assert '"256": {' in text and '"us_v1"' in text
+    for n in (32, 128, 256):      # scramble, then reload from the file
+        for k in range(KINDS):
+            gpu.plan_variant(n, k, 1 - chosen[n][k])
+    gpu.fpga_final()
+    assert gpu.fpga_initialize("cuda:0", path, False) == 0
+    assert {n: [gpu.plan_variant(n, k) for k in range(KINDS)] for n in (32, 128, 256)} == chosen
+    gpu.fpga_final()
+    assert gpu.fpga_initialize("cuda:0", "convgpu_plans.json", False) == 0
+
+
+def test_initialize_ignores_a_file_that_is_not_a_plan_cache(gpu, restore_plans, tmp_path):
+    p = tmp_path / "kernel.aocx"
+    p.write_bytes(os.urandom(4096))
+    gpu.fpga_final()
+    assert gpu.fpga_initialize("cuda:0", str(p), False) == 0
+    gpu.fpga_final()
+    assert gpu.fpga_initialize("cuda:0", "convgpu_plans.json", False) == 0
