@@ -36,6 +36,7 @@ TENSOR_SPLIT = 1 << 3
 TENSOR_BF16X3 = 1 << 4
 UNEVEN_PER_JOB = 1 << 5
 UNEVEN_QUEUE = 1 << 6
+HOST_SLABS = 1 << 7
 
 OK, EINVAL, ENOTINIT, ECUDA, ENOMEM, EUNSUPPORTED = 0, -1, -2, -3, -4, -5
 

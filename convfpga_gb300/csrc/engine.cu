@@ -41,6 +41,7 @@ constexpr unsigned kFlagTensorSplit = 1u << 3;
 constexpr unsigned kFlagTensorBf16x3 = 1u << 4;
 constexpr unsigned kFlagUnevenPerJob = 1u << 5;
 constexpr unsigned kFlagUnevenQueue = 1u << 6;
+constexpr unsigned kFlagHostSlabs = 1u << 7;
 
 constexpr int kErrInval = -1;
 constexpr int kErrNotInit = -2;
@@ -433,6 +434,134 @@ float ms_between(cudaEvent_t a, cudaEvent_t b) {
 }
 }  // namespace
 
+// Host-buffer batch with slab-granular overlap (CONVGPU_HOST_SLABS, cubes of 32 MiB and
+// more): each cube is copied in z-slabs; the x / y passes of a slab start as soon as it
+// lands (planes are independent for those axes), the fused z pass runs once per cube,
+// and the inverse y / x passes hand finished slabs to the device-to-host stream one by
+// one, so pipeline fill and drain shrink from a cube to a slab. On GB300 the 16-32 MiB
+// slab copies move fewer bytes per second than whole-cube copies, and the whole-cube
+// pipeline measured faster end to end (599 vs 575 conv/s at 256^3 x 4), so it stays the
+// default. Returns the error of the first failing call.
+static cudaError_t conv_host_slabs(unsigned n, const float2 *sig, const float2 *filt, float2 *out, unsigned how_many,
+                                   bool per_signal, float scale, int mode, Timing &t) {
+  const size_t V = (size_t)n * n * n;
+  const size_t vbytes = V * sizeof(float2);
+  const int slab = n >= 512 ? 16 : 32;  // planes per slab: 16 MiB at 256^3, 32 MiB at 512^3
+  const int nslab = (int)n / slab;
+  const size_t selems = (size_t)slab * n * n;
+  const unsigned nbuf = std::min(3u, how_many);
+  cudaError_t e = cudaSuccess;
+  for (unsigned b = 0; b < nbuf && e == cudaSuccess; ++b) {
+    e = g.hio[b].ensure(vbytes);
+    if (e == cudaSuccess && per_signal) e = g.hfio[b].ensure(vbytes);
+  }
+  if (e == cudaSuccess && !per_signal) e = g.hfilt.ensure(vbytes);
+  if (e != cudaSuccess) return e;
+  EvPool pool;
+  std::vector<cudaEvent_t> in((size_t)how_many * nslab), done((size_t)how_many * nslab), freed(nbuf);
+  for (auto &v : in) v = pool.get();
+  for (auto &v : done) v = pool.get();
+  for (auto &v : freed) v = pool.get();
+  std::vector<cudaEvent_t> h0(how_many), h1(how_many), c0(how_many), cm(how_many), c1(how_many), d0(how_many),
+      d1(how_many);
+  for (unsigned c = 0; c < how_many; ++c) {
+    h0[c] = pool.get(), h1[c] = pool.get(), c0[c] = pool.get(), cm[c] = pool.get(), c1[c] = pool.get();
+    d0[c] = pool.get(), d1[c] = pool.get();
+  }
+  cudaEvent_t f0 = pool.get(), f1 = pool.get(), f2 = pool.get();
+  float2 *fspec = (float2 *)g.hfilt.p;
+  if (!per_signal) {
+    cudaEventRecord(f0, g.sh2d);
+    e = cudaMemcpyAsync(fspec, filt, vbytes, cudaMemcpyHostToDevice, g.sh2d);
+    cudaEventRecord(f1, g.sh2d);
+    cudaStreamWaitEvent(g.sc, f1, 0);
+    if (e == cudaSuccess) e = enqueue_filter((int)n, fspec, fspec, 1, false, g.sc);
+    cudaEventRecord(f2, g.sc);
+  }
+  auto planes = [&](int axis, int op, float2 *p, float sc) {
+    if (e != cudaSuccess) return;
+    e = launch_axis_pass_planes((int)n, axis, op, p, p, slab, sc, g.tw512, g.sc);
+    if (e == cudaSuccess) count_launches(1);
+  };
+  // Downloads of cube c are enqueued after the uploads of cube c + 1 (see bridge_conv_host).
+  auto out_cube = [&](unsigned c) {
+    const unsigned b = c % nbuf;
+    float2 *io = (float2 *)g.hio[b].p;
+    cudaStreamWaitEvent(g.sd2h, done[c * nslab], 0);
+    cudaEventRecord(d0[c], g.sd2h);
+    for (int k = 0; k < nslab && e == cudaSuccess; ++k) {
+      if (k) cudaStreamWaitEvent(g.sd2h, done[c * nslab + k], 0);
+      e = cudaMemcpyAsync(out + c * V + k * selems, io + k * selems, selems * sizeof(float2), cudaMemcpyDeviceToHost,
+                          g.sd2h);
+    }
+    cudaEventRecord(d1[c], g.sd2h);
+    cudaEventRecord(freed[b], g.sd2h);
+  };
+  for (unsigned c = 0; c < how_many && e == cudaSuccess; ++c) {
+    const unsigned b = c % nbuf;
+    float2 *io = (float2 *)g.hio[b].p;
+    float2 *fio = per_signal ? (float2 *)g.hfio[b].p : nullptr;
+    if (c >= nbuf) cudaStreamWaitEvent(g.sh2d, freed[b], 0);
+    cudaEventRecord(h0[c], g.sh2d);
+    for (int k = 0; k < nslab && e == cudaSuccess; ++k) {
+      e = cudaMemcpyAsync(io + k * selems, sig + c * V + k * selems, selems * sizeof(float2), cudaMemcpyHostToDevice,
+                          g.sh2d);
+      if (e == cudaSuccess && per_signal)
+        e = cudaMemcpyAsync(fio + k * selems, filt + c * V + k * selems, selems * sizeof(float2),
+                            cudaMemcpyHostToDevice, g.sh2d);
+      cudaEventRecord(in[c * nslab + k], g.sh2d);
+    }
+    cudaEventRecord(h1[c], g.sh2d);
+    if (c > 0) out_cube(c - 1);
+    cudaStreamWaitEvent(g.sc, in[c * nslab], 0);
+    cudaEventRecord(c0[c], g.sc);
+    for (int k = 0; k < nslab && e == cudaSuccess; ++k) {
+      if (k) cudaStreamWaitEvent(g.sc, in[c * nslab + k], 0);
+      if (per_signal) {
+        planes(0, OP_FWD, fio + k * selems, 1.f);
+        planes(1, OP_FWD, fio + k * selems, 1.f);
+      }
+      planes(0, OP_FWD, io + k * selems, 1.f);
+      planes(1, OP_FWD, io + k * selems, 1.f);
+    }
+    if (e == cudaSuccess)
+      e = pass((int)n, 2, per_signal ? OP_CONV_FZ : OP_CONV, io, io, per_signal ? fio : fspec,
+               per_signal ? (long long)V : 0, 1, 1.f, g.sc, 0);
+    if (e == cudaSuccess) count_launches(1);
+    cudaEventRecord(cm[c], g.sc);
+    for (int k = 0; k < nslab && e == cudaSuccess; ++k) {
+      planes(1, OP_INV, io + k * selems, 1.f);
+      planes(0, OP_INV, io + k * selems, scale);
+      cudaEventRecord(done[c * nslab + k], g.sc);
+    }
+    cudaEventRecord(c1[c], g.sc);
+  }
+  if (e == cudaSuccess) out_cube(how_many - 1);
+  cudaError_t es = cudaStreamSynchronize(g.sd2h);
+  cudaError_t es2 = cudaStreamSynchronize(g.sc);
+  cudaError_t es3 = cudaStreamSynchronize(g.sh2d);
+  if (e == cudaSuccess) e = es != cudaSuccess ? es : (es2 != cudaSuccess ? es2 : es3);
+  if (e != cudaSuccess) return e;
+  if (!per_signal) {
+    t.filter_pcie_wr_t = ms_between(f0, f1);
+    t.filter_exec_t = ms_between(f1, f2);
+  }
+  double inv = 0.0;
+  for (unsigned c = 0; c < how_many; ++c) {
+    t.sig_pcie_wr_t += ms_between(h0[c], h1[c]);
+    t.sig_exec_t += ms_between(c0[c], cm[c]);
+    inv += ms_between(cm[c], c1[c]);
+    t.sig_pcie_rd_t += ms_between(d0[c], d1[c]);
+  }
+  if (mode == HOST_BATCH) {
+    t.sig_exec_t += inv;
+    t.siginv_exec_t = ms_between(c0[0], c1[how_many - 1]);
+  } else {
+    t.siginv_exec_t = inv;
+  }
+  return cudaSuccess;
+}
+
 Timing bridge_conv_host(unsigned n, const void *sig, const void *filt, void *out, unsigned how_many,
                         unsigned flags, int mode) {
   Timing t{0, 0, 0, 0, 0, 0, false};
@@ -460,6 +589,20 @@ Timing bridge_conv_host(unsigned n, const void *sig, const void *filt, void *out
   const size_t V = (size_t)n * n * n;
   const size_t vbytes = V * sizeof(float2);
   const float scale = (flags & kFlagNormalize) ? (float)(1.0 / ((double)V)) : 1.0f;
+  if (!tc && (flags & kFlagHostSlabs) && vbytes >= (size_t(32) << 20)) {
+    cudaError_t e = conv_host_slabs(n, (const float2 *)sig, (const float2 *)filt, (float2 *)out, how_many, per_signal,
+                                    scale, mode, t);
+    if (e != cudaSuccess) {
+      cuda_fail(e, "host pipeline");
+      return t;
+    }
+    if (const unsigned st = read_and_clear_device_status()) {
+      set_err("device status " + std::to_string(st) + ": a kernel gave up waiting for its tile load");
+      return t;
+    }
+    t.valid = true;
+    return t;
+  }
   // Signals per chunk: at least one cube, about 64 MiB per chunk otherwise.
   const unsigned per_chunk = (unsigned)std::max<size_t>(1, std::min<size_t>(how_many, (64u << 20) / vbytes));
   const unsigned nchunks = (how_many + per_chunk - 1) / per_chunk;
@@ -501,6 +644,20 @@ Timing bridge_conv_host(unsigned n, const void *sig, const void *filt, void *out
     cudaEventRecord(f2, g.sc);
   }
 
+  // Downloads of chunk c are enqueued after the uploads of chunk c + 1, so a download
+  // waiting for its compute never sits ahead of the next upload in a copy queue.
+  auto out_chunk = [&](unsigned c) {
+    const unsigned b = c % nbuf;
+    const unsigned first = c * per_chunk;
+    const unsigned cnt = std::min(per_chunk, how_many - first);
+    cudaStreamWaitEvent(g.sd2h, c1[c], 0);
+    cudaEventRecord(d0[c], g.sd2h);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync((float2 *)out + (size_t)first * V, g.hio[b].p, cnt * vbytes, cudaMemcpyDeviceToHost,
+                          g.sd2h);
+    cudaEventRecord(d1[c], g.sd2h);
+    cudaEventRecord(freed[b], g.sd2h);
+  };
   for (unsigned c = 0; c < nchunks && e == cudaSuccess; ++c) {
     const unsigned b = c % nbuf;
     const unsigned first = c * per_chunk;
@@ -514,6 +671,7 @@ Timing bridge_conv_host(unsigned n, const void *sig, const void *filt, void *out
                           cudaMemcpyHostToDevice, g.sh2d);
     cudaEventRecord(h1[c], g.sh2d);
     if (e != cudaSuccess) break;
+    if (c > 0) out_chunk(c - 1);
     cudaStreamWaitEvent(g.sc, h1[c], 0);
     cudaEventRecord(c0[c], g.sc);
     if (per_signal) {
@@ -525,13 +683,8 @@ Timing bridge_conv_host(unsigned n, const void *sig, const void *filt, void *out
       e = enqueue_signals(n, io, io, fspec, 0, OP_CONV, cnt, scale, g.sc, cm[c], tc);
     }
     cudaEventRecord(c1[c], g.sc);
-    if (e != cudaSuccess) break;
-    cudaStreamWaitEvent(g.sd2h, c1[c], 0);
-    cudaEventRecord(d0[c], g.sd2h);
-    e = cudaMemcpyAsync((float2 *)out + (size_t)first * V, io, cnt * vbytes, cudaMemcpyDeviceToHost, g.sd2h);
-    cudaEventRecord(d1[c], g.sd2h);
-    cudaEventRecord(freed[b], g.sd2h);
   }
+  if (e == cudaSuccess) out_chunk(nchunks - 1);
   cudaError_t es = cudaStreamSynchronize(g.sd2h);
   cudaError_t es2 = cudaStreamSynchronize(g.sc);
   cudaError_t es3 = cudaStreamSynchronize(g.sh2d);

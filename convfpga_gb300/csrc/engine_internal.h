@@ -38,6 +38,10 @@ constexpr int kKindRows = 0, kKindStrided = 1, kKindConv = 2, kKindConvFz = 3, k
 int pass_kind(int axis, int op);
 void set_pass_variant(int n, int kind, int variant);
 int get_pass_variant(int n, int kind);
+// x or y pass (FWD / INV) over `nplanes` consecutive N x N planes starting at src / dst
+// (a slab of a cube; planes are independent for these axes).
+cudaError_t launch_axis_pass_planes(int n, int axis, int op, const float2 *src, float2 *dst, int nplanes, float scale,
+                                    const float2 *tw512, cudaStream_t s);
 // launch_axis_pass with an explicit shape variant (the autotuner times both).
 cudaError_t launch_axis_pass_variant(int n, int axis, int op, const float2 *src, float2 *dst, const float2 *filt,
                                      long long filt_vol_elems, int nvol, float scale, const float2 *tw512,

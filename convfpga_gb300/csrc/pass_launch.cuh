@@ -39,7 +39,8 @@ struct PassReq {
                 // kModeTable (table-mode TMA), kModeGather (register-gather kernels)
   int axis;     // 0 x, 1 y, 2 z
   int op;       // OP_FWD, OP_INV, OP_CONV, OP_CONV_FZ
-  int nvol;
+  int nvol;     // cubes (z pass); the x / y passes use nplanes
+  int nplanes;  // x / y passes: planes of N*N points to transform (a cube is N planes)
   int variant;  // shape variant 0 / 1
   PassArgs a;
   cudaStream_t s;
@@ -67,7 +68,7 @@ static cudaError_t set_smem_once(K kern, int smem, bool &done) {
 
 // Register-gather kernels (shape variant 0): any 8-byte aligned operands.
 template <int N, bool CONTIG, int OP>
-static cudaError_t launch_gather(PassArgs a, int nvol, cudaStream_t s) {
+static cudaError_t launch_gather(PassArgs a, int nvol, int nplanes, cudaStream_t s) {
   using S = Shape<N, 0>;
   constexpr int E = S::E;
   constexpr int COLS = CONTIG ? S::XC : S::SC;
@@ -78,7 +79,11 @@ static cudaError_t launch_gather(PassArgs a, int nvol, cudaStream_t s) {
   if (e != cudaSuccess) return e;
   a.groups_x = N / S::SC;
   a.groups_per_vol = N * (N / S::SC);
-  const long long blocks = CONTIG ? (long long)nvol * N * N / COLS : (long long)nvol * a.groups_per_vol;
+  // x / y passes: nplanes planes (a plane is N rows, or N / SC y-tiles); z pass: cubes
+  const long long blocks = CONTIG ? (long long)nplanes * N / COLS
+                                  : (OP == OP_FWD || OP == OP_INV) && a.axis_stride == N
+                                        ? (long long)nplanes * (N / S::SC)
+                                        : (long long)nvol * a.groups_per_vol;
   if (blocks <= 0 || blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
   kern<<<(unsigned)blocks, COLS * (N / E), smem, s>>>(a);
   return cudaGetLastError();
@@ -98,9 +103,9 @@ static cudaError_t launch_rows(const PassReq &r) {
   std::memset(&m, 0, sizeof(m));
   if (r.mode != kModeTable) {
     if ((reinterpret_cast<uintptr_t>(r.a.dst) & 15u) != 0) return cudaErrorNotSupported;
-    if (!encode_rows_map(&m, r.a.src, N, (long long)r.nvol * N * N, XC)) return cudaErrorNotSupported;
+    if (!encode_rows_map(&m, r.a.src, N, (long long)r.nplanes * N, XC)) return cudaErrorNotSupported;
   }
-  const long long blocks = (long long)r.nvol * N * N / XC;
+  const long long blocks = r.mode == kModeTable ? (long long)r.nvol * N * N / XC : (long long)r.nplanes * N / XC;
   if (blocks <= 0 || blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
   kern<<<(unsigned)blocks, XC * (N / E), smem, r.s>>>(m, r.a);
   return cudaGetLastError();
@@ -127,13 +132,15 @@ static cudaError_t launch_strided(const PassReq &r) {
   std::memset(&mfilt, 0, sizeof(mfilt));
   if (r.mode != kModeTable) {
     if ((reinterpret_cast<uintptr_t>(a.dst) & 15u) != 0) return cudaErrorNotSupported;
-    if (!encode_cube_map(&msrc, a.src, N, (long long)r.nvol * N, r.axis, COLS)) return cudaErrorNotSupported;
+    const long long planes = r.axis == 1 ? (long long)r.nplanes : (long long)r.nvol * N;
+    if (!encode_cube_map(&msrc, a.src, N, planes, r.axis, COLS)) return cudaErrorNotSupported;
     if (HAS_F) {
       const long long fplanes = a.filt_vol_elems ? (long long)r.nvol * N : (long long)N;
       if (!encode_cube_map(&mfilt, a.filt, N, fplanes, r.axis, COLS)) return cudaErrorNotSupported;
     }
   }
-  const long long blocks = (long long)r.nvol * a.groups_per_vol;
+  const long long blocks = (r.axis == 1 && r.mode != kModeTable) ? (long long)r.nplanes * (N / COLS)
+                                                                  : (long long)r.nvol * a.groups_per_vol;
   if (blocks <= 0 || blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
   kern<<<(unsigned)blocks, COLS * (N / E), smem, r.s>>>(msrc, mfilt, a, r.axis);
   return cudaGetLastError();
@@ -160,17 +167,17 @@ static cudaError_t launch_gather_op(const PassReq &r) {
   PassArgs a = r.a;
   a.vol_elems = (long long)N * N * N;
   if (r.axis == 0) {
-    if (r.op == OP_FWD) return launch_gather<N, true, OP_FWD>(a, r.nvol, r.s);
-    if (r.op == OP_INV) return launch_gather<N, true, OP_INV>(a, r.nvol, r.s);
+    if (r.op == OP_FWD) return launch_gather<N, true, OP_FWD>(a, r.nvol, r.nplanes, r.s);
+    if (r.op == OP_INV) return launch_gather<N, true, OP_INV>(a, r.nvol, r.nplanes, r.s);
     return cudaErrorInvalidValue;
   }
   a.axis_stride = r.axis == 1 ? N : (long long)N * N;
   a.plane_pitch = r.axis == 1 ? (long long)N * N : N;
   switch (r.op) {
-    case OP_FWD: return launch_gather<N, false, OP_FWD>(a, r.nvol, r.s);
-    case OP_INV: return launch_gather<N, false, OP_INV>(a, r.nvol, r.s);
-    case OP_CONV: return launch_gather<N, false, OP_CONV>(a, r.nvol, r.s);
-    case OP_CONV_FZ: return launch_gather<N, false, OP_CONV_FZ>(a, r.nvol, r.s);
+    case OP_FWD: return launch_gather<N, false, OP_FWD>(a, r.nvol, r.nplanes, r.s);
+    case OP_INV: return launch_gather<N, false, OP_INV>(a, r.nvol, r.nplanes, r.s);
+    case OP_CONV: return launch_gather<N, false, OP_CONV>(a, r.nvol, r.nplanes, r.s);
+    case OP_CONV_FZ: return launch_gather<N, false, OP_CONV_FZ>(a, r.nvol, r.nplanes, r.s);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -197,6 +197,7 @@ cudaError_t launch_axis_pass_variant(int n, int axis, int op, const float2 *src,
   r.axis = axis;
   r.op = op;
   r.nvol = nvol;
+  r.nplanes = nvol * n;
   r.variant = variant;
   r.a = make_args(n, src, dst, filt, filt_vol_elems, scale, tw512);
   r.s = s;
@@ -208,6 +209,22 @@ cudaError_t launch_axis_pass(int n, int axis, int op, const float2 *src, float2 
                              cudaStream_t s) {
   return launch_axis_pass_variant(n, axis, op, src, dst, filt, filt_vol_elems, nvol, scale, tw512, s,
                                   get_pass_variant(n, pass_kind(axis, op)));
+}
+
+cudaError_t launch_axis_pass_planes(int n, int axis, int op, const float2 *src, float2 *dst, int nplanes, float scale,
+                                    const float2 *tw512, cudaStream_t s) {
+  if (nplanes <= 0) return cudaSuccess;
+  if (axis > 1 || (op != OP_FWD && op != OP_INV) || size_index(n) < 0) return cudaErrorInvalidValue;
+  PassReq r{};
+  r.mode = g_use_tma ? kModeTma : kModeGather;
+  r.axis = axis;
+  r.op = op;
+  r.nvol = (nplanes + n - 1) / n;
+  r.nplanes = nplanes;
+  r.variant = get_pass_variant(n, pass_kind(axis, op));
+  r.a = make_args(n, src, dst, nullptr, 0, scale, tw512);
+  r.s = s;
+  return dispatch(n, r);
 }
 
 cudaError_t prepare_table_launches(int n) {
@@ -233,6 +250,7 @@ cudaError_t launch_axis_pass_table(int n, int axis, int op, const CUtensorMap *m
   r.axis = axis;
   r.op = op;
   r.nvol = nvol;
+  r.nplanes = nvol * n;
   r.a = make_args(n, nullptr, nullptr, nullptr, (long long)n * n * n, scale, tw512);
   r.a.maps = maps;
   r.a.fmaps = fmaps;
@@ -254,6 +272,7 @@ cudaError_t launch_axis_pass_tc(int n, int axis, int op, const float2 *src, floa
   r.axis = axis;
   r.op = op;
   r.nvol = nvol;
+  r.nplanes = nvol * n;
   r.a = make_args(n, src, dst, filt, filt_vol_elems, scale, tw512);
   r.s = s;
   const cudaError_t e = launch_tc256_entry(r, prec == kTcBf16x3 ? 1 : 0);

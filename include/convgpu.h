@@ -27,6 +27,7 @@ extern "C" {
 #define CONVGPU_TENSOR_BF16X3 (1u << 4)        /* tensor-core path, BF16x3 split (implies TENSOR_SPLIT) */
 #define CONVGPU_UNEVEN_PER_JOB (1u << 5)       /* uneven batch: one job at a time */
 #define CONVGPU_UNEVEN_QUEUE (1u << 6)         /* uneven batch: one persistent work-queue launch */
+#define CONVGPU_HOST_SLABS (1u << 7)           /* host batch: stream cubes >= 32 MiB in z-slabs */
 
 /* Status codes */
 #define CONVGPU_OK 0

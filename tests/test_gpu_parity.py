@@ -273,3 +273,38 @@ def test_uneven_in_place_and_distinct_offsets(gpu):
     for i, n in enumerate(sizes):
         ref = conv3d(sigs[i], filts[i], "fp32", engine="pocketfft")
         assert snr_db(ref, oh[offs[i]:offs[i + 1]].reshape(n, n, n)) > SNR_DB
+
+
+@pytest.mark.parametrize("per_signal,b,slabs", [(True, 4, True), (False, 2, True), (True, 4, False)])
+def test_host_pipelines_256(gpu, per_signal, b, slabs):
+    """256^3 cubes through the host pipelines: whole-cube chunks (default) and, with
+    CONVGPU_HOST_SLABS, z-slab streaming (x / y passes per slab as it lands, fused z per
+    cube, inverse per slab, slab downloads); 4 cubes wrap the 3-buffer ring."""
+    rng = np.random.default_rng(256 + b)
+    n = 256
+    sig = _c64(rng, (b, n, n, n))
+    filt = _c64(rng, (b, n, n, n)) if per_signal else _c64(rng, (n, n, n))
+    out = np.zeros_like(sig)
+    extra = gpu.HOST_SLABS if slabs else 0
+    if per_signal:
+        t = gpu.conv3d_host(n, sig, filt, out, b, gpu.FILTER_PER_SIGNAL | gpu.NORMALIZE | extra)
+        ref = conv3d(sig, filt, "fp32", normalize=True, engine="pocketfft")
+    else:
+        t = gpu.conv3d_host(n, sig, filt, out, b, extra)
+        ref = conv3d(sig, filt, "fp32", engine="pocketfft")
+    assert t.valid, gpu.last_error()
+    assert t.sig_pcie_wr_t > 0 and t.sig_pcie_rd_t > 0 and t.sig_exec_t > 0
+    for i in range(b):
+        assert snr_db(ref[i], out[i]) > SNR_DB
+
+
+@pytest.mark.slow
+def test_host_slab_pipeline_512(gpu):
+    rng = np.random.default_rng(5120)
+    n = 512
+    sig = _c64(rng, (1, n, n, n))
+    filt = gaussian_filter(n, 6.0)
+    out = np.zeros_like(sig)
+    t = gpu.conv3d_host(n, sig, filt, out, 1, gpu.HOST_SLABS)
+    assert t.valid, gpu.last_error()
+    assert snr_db(conv3d(sig, filt, "fp32", engine="pocketfft"), out) > SNR_DB
