@@ -278,7 +278,7 @@ def launch_count() -> int:
     return int(load_library().convgpu_launch_count())
 
 
-PASS_SLOTS = 12
+PASS_SLOTS = 14
 PASS_AXES = ("x", "y", "z")
 PASS_OPS = ("fwd", "inv", "conv", "conv_fz")
 
@@ -300,11 +300,12 @@ def pass_timing_read() -> dict:
     out = {}
     for i in range(PASS_SLOTS):
         if cnt[i]:
-            out[f"{PASS_AXES[i // 4]}-{PASS_OPS[i % 4]}"] = {"ms": ms[i], "launches": int(cnt[i]), "bytes": by[i]}
+            name = f"{PASS_AXES[i // 4]}-{PASS_OPS[i % 4]}" if i < 12 else ("xy-fwd", "xy-inv")[i - 12]
+            out[name] = {"ms": ms[i], "launches": int(cnt[i]), "bytes": by[i]}
     return out
 
 
-PLAN_KINDS = ("rows", "strided", "conv", "conv_fz")
+PLAN_KINDS = ("rows", "strided", "conv", "conv_fz", "xy")
 
 
 def autotune(sizes, write_cache: bool = True) -> None:

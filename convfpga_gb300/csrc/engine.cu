@@ -196,7 +196,7 @@ static int ensure_init_locked() {
 // Optional per-pass timing: events around every pass on its own stream, summed per
 // (axis, op) slot with the pass's algorithmic bytes (one read + one write of every
 // cube, plus one read of the filter operand for the fused z pass).
-constexpr int kSlots = 12;  // slot = axis * 4 + op
+constexpr int kSlots = 14;  // slot = axis * 4 + op; 12 / 13: fused x+y forward / inverse
 struct PassRec {
   int slot;
   double bytes;
@@ -224,6 +224,33 @@ static cudaError_t pass(int n, int axis, int op, const float2 *src, float2 *dst,
   return e;
 }
 
+// Fused x + y pass (N = 256, 8-CTA clusters). Returns cudaErrorNotSupported when it
+// cannot run, in which case the caller runs the x and y passes separately.
+static cudaError_t pass_xy(int n, const float2 *src, float2 *dst, int nvol, bool inverse, float scale,
+                           cudaStream_t s) {
+  PassRec r{12 + (inverse ? 1 : 0), 0.0, nullptr, nullptr};
+  if (g_prof) {
+    r.bytes = 2.0 * (double)n * n * n * 8.0 * nvol;
+    cudaEventCreate(&r.a);
+    cudaEventCreate(&r.b);
+    cudaEventRecord(r.a, s);
+  }
+  cudaError_t e = launch_xy_pass(n, src, dst, nvol * n, inverse, scale, g.tw512, s);
+  if (g_prof) {
+    cudaEventRecord(r.b, s);
+    if (e == cudaSuccess) {
+      g_prof_recs.push_back(r);
+    } else {
+      cudaEventDestroy(r.a);
+      cudaEventDestroy(r.b);
+    }
+  }
+  if (e == cudaSuccess) count_launches(1);
+  return e;
+}
+
+static bool use_xy(int n, int tc) { return tc == 0 && n == 256 && get_pass_variant(n, kKindXy) == 1; }
+
 // ------------------------------------------------------------------ pass sequences
 #define CG_TRY(expr)                        \
   do {                                      \
@@ -235,8 +262,12 @@ static cudaError_t pass(int n, int axis, int op, const float2 *src, float2 *dst,
 // Filter spectra of `count` filters (x, y and, unless xy_only, z passes) into spec.
 static cudaError_t enqueue_filter(int n, const float2 *filt, float2 *spec, int count, bool xy_only,
                                   cudaStream_t s, int tc = 0) {
-  CG_TRY(pass(n, 0, OP_FWD, filt, spec, nullptr, 0, count, 1.f, s, tc));
-  CG_TRY(pass(n, 1, OP_FWD, spec, spec, nullptr, 0, count, 1.f, s, tc));
+  cudaError_t xe = use_xy(n, tc) ? pass_xy(n, filt, spec, count, false, 1.f, s) : cudaErrorNotSupported;
+  if (xe != cudaSuccess && xe != cudaErrorNotSupported) return xe;
+  if (xe == cudaErrorNotSupported) {
+    CG_TRY(pass(n, 0, OP_FWD, filt, spec, nullptr, 0, count, 1.f, s, tc));
+    CG_TRY(pass(n, 1, OP_FWD, spec, spec, nullptr, 0, count, 1.f, s, tc));
+  }
   if (!xy_only) CG_TRY(pass(n, 2, OP_FWD, spec, spec, nullptr, 0, count, 1.f, s, tc));
   return cudaSuccess;
 }
@@ -246,10 +277,20 @@ static cudaError_t enqueue_filter(int n, const float2 *filt, float2 *spec, int c
 static cudaError_t enqueue_signals(int n, const float2 *sig, float2 *out, const float2 *spec,
                                    long long spec_vol, int fop, int nsig, float scale, cudaStream_t s,
                                    cudaEvent_t mid, int tc = 0) {
-  CG_TRY(pass(n, 0, OP_FWD, sig, out, nullptr, 0, nsig, 1.f, s, tc));
-  CG_TRY(pass(n, 1, OP_FWD, out, out, nullptr, 0, nsig, 1.f, s, tc));
+  cudaError_t xe = use_xy(n, tc) ? pass_xy(n, sig, out, nsig, false, 1.f, s) : cudaErrorNotSupported;
+  if (xe != cudaSuccess && xe != cudaErrorNotSupported) return xe;
+  const bool fused = xe == cudaSuccess;
+  if (!fused) {
+    CG_TRY(pass(n, 0, OP_FWD, sig, out, nullptr, 0, nsig, 1.f, s, tc));
+    CG_TRY(pass(n, 1, OP_FWD, out, out, nullptr, 0, nsig, 1.f, s, tc));
+  }
   CG_TRY(pass(n, 2, fop, out, out, spec, spec_vol, nsig, 1.f, s, tc));
   if (mid) cudaEventRecord(mid, s);
+  if (fused) {
+    const cudaError_t e = pass_xy(n, out, out, nsig, true, scale, s);
+    if (e == cudaSuccess) return cudaSuccess;
+    if (e != cudaErrorNotSupported) return e;
+  }
   CG_TRY(pass(n, 1, OP_INV, out, out, nullptr, 0, nsig, 1.f, s, tc));
   CG_TRY(pass(n, 0, OP_INV, out, out, nullptr, 0, nsig, scale, s, tc));
   return cudaSuccess;
@@ -726,7 +767,7 @@ Timing bridge_conv_host(unsigned n, const void *sig, const void *filt, void *out
 // (src/fft_conv3D.cpp:85-112): one line per cube size with the shape variant chosen for
 // each pass kind and the timings (microseconds per launch, variants 0 and 1) it was
 // chosen from.
-static const char *kKindNames[kPassKinds] = {"rows", "strided", "conv", "conv_fz"};
+static const char *kKindNames[kPassKinds] = {"rows", "strided", "conv", "conv_fz", "xy"};
 
 static void load_plan_cache(const std::string &path) {
   FILE *f = std::fopen(path.c_str(), "r");
@@ -804,6 +845,32 @@ int bridge_autotune(const unsigned *sizes, unsigned count, int write_cache) {
     TuneRow row{};
     row.n = n;
     for (int k = 0; k < kPassKinds && err == cudaSuccess; ++k) {
+      if (k == kKindXy) {
+        // separate x and y passes (variant 0) against the fused cluster pass (variant 1)
+        row.us[0][k] = row.us[row.choice[kKindRows]][kKindRows] + row.us[row.choice[kKindStrided]][kKindStrided];
+        row.us[1][k] = 1e30;
+        if (n == 256) {
+          for (int w = 0; w < 2 && err == cudaSuccess; ++w) {
+            err = launch_xy_pass(n, data, data, nvol * n, false, 1.f, g.tw512, s);
+            if (err == cudaErrorNotSupported) break;
+          }
+          if (err == cudaSuccess) {
+            cudaEventRecord(e0, s);
+            for (int t = 0; t < 5 && err == cudaSuccess; ++t) err = launch_xy_pass(n, data, data, nvol * n, false, 1.f, g.tw512, s);
+            cudaEventRecord(e1, s);
+            cudaEventSynchronize(e1);
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            row.us[1][k] = 1000.0 * ms / 5.0;
+            count_launches(7);
+          } else if (err == cudaErrorNotSupported) {
+            err = cudaSuccess;
+          }
+        }
+        row.choice[k] = row.us[1][k] < row.us[0][k] ? 1 : 0;
+        set_pass_variant(n, k, row.choice[k]);
+        continue;
+      }
       const int axis = k == kKindRows ? 0 : (k == kKindStrided ? 1 : 2);
       const int op = k == kKindConv ? OP_CONV : (k == kKindConvFz ? OP_CONV_FZ : OP_FWD);
       const long long fv = k == kKindConvFz ? (long long)V : 0;

@@ -34,10 +34,14 @@ void set_tma_enabled(bool on);
 
 // Plan table: shape variant (0 / 1) per cube size and pass kind, chosen by the
 // autotuner and recorded in the plan cache.
-constexpr int kKindRows = 0, kKindStrided = 1, kKindConv = 2, kKindConvFz = 3, kPassKinds = 4;
+constexpr int kKindRows = 0, kKindStrided = 1, kKindConv = 2, kKindConvFz = 3, kKindXy = 4, kPassKinds = 5;
 int pass_kind(int axis, int op);
 void set_pass_variant(int n, int kind, int variant);
 int get_pass_variant(int n, int kind);
+// Fused x + y pass over `nplanes` planes (N = 256 only; cudaErrorNotSupported otherwise
+// or when tensor maps cannot describe the operands). Plan kind kKindXy, variant 1.
+cudaError_t launch_xy_pass(int n, const float2 *src, float2 *dst, int nplanes, bool inverse, float scale,
+                           const float2 *tw512, cudaStream_t s);
 // x or y pass (FWD / INV) over `nplanes` consecutive N x N planes starting at src / dst
 // (a slab of a cube; planes are independent for these axes).
 cudaError_t launch_axis_pass_planes(int n, int axis, int op, const float2 *src, float2 *dst, int nplanes, float scale,

@@ -29,7 +29,7 @@ template <> struct Shape<64, 1> { static constexpr int E = 16, XC = 16, SC = 16;
 template <> struct Shape<128, 0> { static constexpr int E = 16, XC = 16, SC = 32; using Plan = Radices<16, 8>; };
 template <> struct Shape<128, 1> { static constexpr int E = 16, XC = 8, SC = 16; using Plan = Radices<8, 16>; };
 template <> struct Shape<256, 0> { static constexpr int E = 16, XC = 8, SC = 16; using Plan = Radices<16, 16>; };
-template <> struct Shape<256, 1> { static constexpr int E = 16, XC = 16, SC = 32; using Plan = Radices<16, 16>; };
+template <> struct Shape<256, 1> { static constexpr int E = 16, XC = 16, SC = 8; using Plan = Radices<16, 16>; };
 template <> struct Shape<512, 0> { static constexpr int E = 16, XC = 4, SC = 16; using Plan = Radices<16, 16, 2>; };
 template <> struct Shape<512, 1> { static constexpr int E = 8, XC = 2, SC = 16; using Plan = Radices<8, 8, 8>; };
 
@@ -224,4 +224,7 @@ cudaError_t prepare_size() {
 namespace convgpu {
 // Tensor-core pass for N = 256 (passes_n256.cu); bf16x3 selects BF16x3 over TF32x3.
 cudaError_t launch_tc256_entry(const PassReq &r, int bf16x3);
+// Fused x + y pass for N = 256 on 8-CTA clusters (passes_n256.cu, xy256.cuh).
+cudaError_t launch_xy256(const float2 *src, float2 *dst, int nplanes, bool inverse, float scale, const float2 *tw512,
+                         unsigned int *status, cudaStream_t s);
 }  // namespace convgpu

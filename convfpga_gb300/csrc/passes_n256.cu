@@ -4,6 +4,8 @@
 #include "pass_launch.cuh"
 #include "tc.cuh"
 
+#include <algorithm>
+
 namespace convgpu {
 template cudaError_t launch_size<256>(const PassReq &);
 template cudaError_t prepare_size<256>();
@@ -69,4 +71,44 @@ cudaError_t launch_tc256_entry(const PassReq &r, int bf16x3) {
   return bf16x3 ? launch_tc256_op<PrecBf16x3>(r.op, r.axis, r.a, r.nvol, r.s)
                 : launch_tc256_op<PrecTf32x3>(r.op, r.axis, r.a, r.nvol, r.s);
 }
+}  // namespace convgpu
+
+#include "xy256.cuh"
+
+namespace convgpu {
+
+// Fused x + y pass over `nplanes` consecutive 256 x 256 planes (see xy256.cuh).
+// cudaErrorNotSupported when the operands cannot be described by a tensor map.
+cudaError_t launch_xy256(const float2 *src, float2 *dst, int nplanes, bool inverse, float scale, const float2 *tw512,
+                         unsigned int *status, cudaStream_t s) {
+  if (nplanes <= 0) return cudaSuccess;
+  if ((reinterpret_cast<uintptr_t>(dst) & 15u) != 0) return cudaErrorNotSupported;
+  CUtensorMap m;
+  if (!encode_rows_map(&m, src, 256, (long long)nplanes * 256, kXyRows)) return cudaErrorNotSupported;
+  auto kern = inverse ? k_xy256<true> : k_xy256<false>;
+  static bool done[2] = {false, false};
+  cudaError_t e = set_smem_once(kern, kXySmem, done[inverse ? 1 : 0]);
+  if (e != cudaSuccess) return e;
+  static int max_clusters[2] = {0, 0};
+  int &mc = max_clusters[inverse ? 1 : 0];
+  if (mc == 0) {
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(kXyCluster * 64, 1, 1);
+    cfg.blockDim = dim3(kXyThreads, 1, 1);
+    cfg.dynamicSmemBytes = kXySmem;
+    int n = 0;
+    if (cudaOccupancyMaxActiveClusters(&n, (const void *)kern, &cfg) != cudaSuccess || n <= 0) {
+      cudaGetLastError();
+      int dev = 0, sms = 0;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      n = std::max(1, sms / kXyCluster);
+    }
+    mc = n;
+  }
+  const int clusters = std::min(mc, nplanes);
+  kern<<<clusters * kXyCluster, kXyThreads, kXySmem, s>>>(m, dst, nplanes, scale, tw512, status);
+  return cudaGetLastError();
+}
+
 }  // namespace convgpu

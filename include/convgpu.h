@@ -123,8 +123,8 @@ unsigned long long convgpu_launch_count(void);
  *           bytes (one read + one write of every cube, plus the filter operand read of
  *           the fused z pass); slot = axis * 4 + op, axis 0/1/2 = x/y/z,
  *           op 0 forward, 1 inverse, 2 z fwd->multiply->inv, 3 same with the filter's
- *           z transform fused in. */
-#define CONVGPU_PASS_SLOTS 12
+ *           z transform fused in; slots 12 / 13: fused x+y pass forward / inverse. */
+#define CONVGPU_PASS_SLOTS 14
 int convgpu_pass_timing(int mode, double *ms, unsigned long long *launches, double *bytes);
 
 /* Waits for all work on the library's device. */
@@ -139,8 +139,9 @@ int convgpu_synchronize(void);
 int convgpu_autotune(const unsigned *sizes, unsigned count, int write_cache);
 
 /* Plan-table entry of cube size N for pass kind (0 x pass, 1 y/z passes, 2 fused z pass,
- * 3 fused z pass with the filter's z transform): sets it to set_to (0 or 1) when
- * set_to >= 0, and returns the current variant (or a negative CONVGPU_E* code). */
+ * 3 fused z pass with the filter's z transform, 4 x and y: 0 separate passes, 1 one fused
+ * pass on 8-CTA clusters, N = 256 only): sets it to set_to (0 or 1) when set_to >= 0, and
+ * returns the current variant (or a negative CONVGPU_E* code). */
 int convgpu_plan_variant(unsigned N, int kind, int set_to);
 
 /* Waits for the device, then returns and clears the library's device status word in

@@ -14,7 +14,7 @@ from oracle import conv3d, snr_db
 pytestmark = pytest.mark.gpu
 torch = pytest.importorskip("torch")
 
-KINDS = 4
+KINDS = 4  # shape-variant kinds; kind 4 (fused x+y) is tested separately
 
 
 def _c64(rng, shape):
@@ -28,7 +28,7 @@ def _c64(rng, shape):
 def restore_plans(gpu):
     yield
     for n in (16, 32, 64, 128, 256, 512):
-        for k in range(KINDS):
+        for k in range(KINDS + 1):
             gpu.plan_variant(n, k, 0)
 
 
@@ -62,6 +62,25 @@ def test_512_variants(gpu, restore_plans, variant):
     for k in range(KINDS):
         gpu.plan_variant(512, k, variant)
     _check(gpu, 512, 1, per_signal=True)
+
+
+@pytest.mark.parametrize("variant", [0, 1])
+def test_fused_xy_pass_256(gpu, restore_plans, variant):
+    """x and y of 256^3 cubes as one pass on 8-CTA clusters (plan kind 4, variant 1),
+    forward and inverse, with shared and per-signal filters, and through the host path."""
+    gpu.plan_variant(256, 4, 1)
+    for k in range(KINDS):
+        gpu.plan_variant(256, k, variant)
+    _check(gpu, 256, 2, per_signal=False)
+    _check(gpu, 256, 3, per_signal=True)
+    rng = np.random.default_rng(99)
+    sig = _c64(rng, (2, 256, 256, 256))
+    filt = _c64(rng, (256, 256, 256))
+    out = np.zeros_like(sig)
+    t = gpu.fpgaf_conv3D_svm_batch(256, sig, filt, out, 2)
+    assert t.valid, gpu.last_error()
+    assert snr_db(conv3d(sig, filt, "fp32", engine="pocketfft"), out) > 120.0
+    assert gpu.device_status() == 0
 
 
 def test_autotune_plan_cache_round_trip(gpu, restore_plans, tmp_path):
