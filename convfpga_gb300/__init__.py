@@ -305,7 +305,7 @@ def pass_timing_read() -> dict:
     return out
 
 
-PLAN_KINDS = ("rows", "strided", "conv", "conv_fz", "xy")
+PLAN_KINDS = ("rows", "strided", "conv", "conv_fz", "xy", "tc")
 
 
 def autotune(sizes, write_cache: bool = True) -> None:

@@ -175,6 +175,8 @@ static int setup_locked(int dev, bool use_svm) {
   }
   const char *no_tma = std::getenv("CONVGPU_DISABLE_TMA");
   set_tma_enabled(!(no_tma && no_tma[0] == '1'));
+  const char *tc05_plain = std::getenv("CONVGPU_TC05_NO_SWIZZLE");
+  set_tc05_swizzle(!(tc05_plain && tc05_plain[0] == '1'));
   g.device = dev;
   g.use_svm = use_svm;
   g.init = true;
@@ -767,7 +769,7 @@ Timing bridge_conv_host(unsigned n, const void *sig, const void *filt, void *out
 // (src/fft_conv3D.cpp:85-112): one line per cube size with the shape variant chosen for
 // each pass kind and the timings (microseconds per launch, variants 0 and 1) it was
 // chosen from.
-static const char *kKindNames[kPassKinds] = {"rows", "strided", "conv", "conv_fz", "xy"};
+static const char *kKindNames[kPassKinds] = {"rows", "strided", "conv", "conv_fz", "xy", "tc"};
 
 static void load_plan_cache(const std::string &path) {
   FILE *f = std::fopen(path.c_str(), "r");
@@ -866,6 +868,33 @@ int bridge_autotune(const unsigned *sizes, unsigned count, int write_cache) {
           } else if (err == cudaErrorNotSupported) {
             err = cudaSuccess;
           }
+        }
+        row.choice[k] = row.us[1][k] < row.us[0][k] ? 1 : 0;
+        set_pass_variant(n, k, row.choice[k]);
+        continue;
+      }
+      if (k == kKindTc) {
+        // tensor-core kernel of the split-TF32 path, timed on its fused z pass
+        for (int v = 0; v < 2; ++v) row.us[v][k] = 0.0;
+        if (n == 256) {
+          const int keep = get_pass_variant(n, k);
+          for (int v = 0; v < 2 && err == cudaSuccess; ++v) {
+            set_pass_variant(n, k, v);
+            auto run = [&]() {
+              return launch_axis_pass_tc(n, 2, OP_CONV_FZ, data, data, spec, (long long)V, nvol, 1.f, g.tw512, s,
+                                         kTcTf32x3);
+            };
+            for (int w = 0; w < 2 && err == cudaSuccess; ++w) err = run();
+            cudaEventRecord(e0, s);
+            for (int t = 0; t < 5 && err == cudaSuccess; ++t) err = run();
+            cudaEventRecord(e1, s);
+            cudaEventSynchronize(e1);
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            row.us[v][k] = 1000.0 * ms / 5.0;
+            count_launches(7);
+          }
+          set_pass_variant(n, k, keep);
         }
         row.choice[k] = row.us[1][k] < row.us[0][k] ? 1 : 0;
         set_pass_variant(n, k, row.choice[k]);

@@ -32,9 +32,14 @@ cudaError_t launch_axis_pass_tc(int n, int axis, int op, const float2 *src, floa
 // Selects the TMA-fed y / z pass kernels (default) or the register-gather kernels.
 void set_tma_enabled(bool on);
 
+// Operand layout of the tcgen05 kernels: 128-byte swizzle (default) or none.
+void set_tc05_swizzle(bool on);
+
 // Plan table: shape variant (0 / 1) per cube size and pass kind, chosen by the
 // autotuner and recorded in the plan cache.
-constexpr int kKindRows = 0, kKindStrided = 1, kKindConv = 2, kKindConvFz = 3, kKindXy = 4, kPassKinds = 5;
+// kKindTc: tensor-core kernel of the split-TF32 path (0 tcgen05, 1 mma.sync), N = 256.
+constexpr int kKindRows = 0, kKindStrided = 1, kKindConv = 2, kKindConvFz = 3, kKindXy = 4, kKindTc = 5,
+              kPassKinds = 6;
 int pass_kind(int axis, int op);
 void set_pass_variant(int n, int kind, int variant);
 int get_pass_variant(int n, int kind);
