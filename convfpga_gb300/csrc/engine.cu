@@ -112,9 +112,11 @@ static cudaError_t upload_twiddles(float2 **dst) {
     const double a = -two_pi * (double)j / 512.0;
     h[j] = make_float2((float)std::cos(a), (float)std::sin(a));
   }
-  cudaError_t e = cudaMalloc(dst, 512 * sizeof(float2));
+  cudaError_t e = cudaMalloc(dst, kTwiddleBufBytes);
   if (e != cudaSuccess) return e;
-  return cudaMemcpy(*dst, h.data(), 512 * sizeof(float2), cudaMemcpyHostToDevice);
+  e = cudaMemcpy(*dst, h.data(), 512 * sizeof(float2), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return e;
+  return tc05_init_consts(*dst, 0);
 }
 
 static void teardown_locked() {
@@ -175,8 +177,8 @@ static int setup_locked(int dev, bool use_svm) {
   }
   const char *no_tma = std::getenv("CONVGPU_DISABLE_TMA");
   set_tma_enabled(!(no_tma && no_tma[0] == '1'));
-  const char *tc05_plain = std::getenv("CONVGPU_TC05_NO_SWIZZLE");
-  set_tc05_swizzle(!(tc05_plain && tc05_plain[0] == '1'));
+  const char *tc05_p = std::getenv("CONVGPU_TC05_PENCILS");
+  set_tc05_pencils(tc05_p ? std::atoi(tc05_p) : 8);
   g.device = dev;
   g.use_svm = use_svm;
   g.init = true;

@@ -32,8 +32,13 @@ cudaError_t launch_axis_pass_tc(int n, int axis, int op, const float2 *src, floa
 // Selects the TMA-fed y / z pass kernels (default) or the register-gather kernels.
 void set_tma_enabled(bool on);
 
-// Operand layout of the tcgen05 kernels: 128-byte swizzle (default) or none.
-void set_tc05_swizzle(bool on);
+// Pencils per CTA of the tcgen05 kernels (8 default, or 16).
+void set_tc05_pencils(int p);
+
+// Twiddle buffer of the engine: 512 twiddles W512^j followed by the constant block of
+// the tcgen05 kernels (B operand hi / lo, W256^j), written by tc05_init_consts.
+constexpr size_t kTwiddleBufBytes = 512 * 8 + 2 * 4096 + 256 * 8;
+cudaError_t tc05_init_consts(float2 *tw, cudaStream_t s);
 
 // Plan table: shape variant (0 / 1) per cube size and pass kind, chosen by the
 // autotuner and recorded in the plan cache.

@@ -2,31 +2,34 @@
 // (tcgen05): operands from shared-memory matrix descriptors, accumulators in tensor
 // memory (TMEM), one thread issuing the MMAs, completion tracked on an mbarrier.
 //
-// A 256-point transform is 16 x 16 (four-step). A CTA holds 16 pencils, i.e. 256
-// instances of each 16-point stage; thread m owns instance m and its A-operand row
+// A 256-point transform is 16 x 16 (four-step). A CTA holds P pencils (P = 8 or 16),
+// i.e. 16 P instances of each 16-point stage; thread m owns instance m and its A row
 //   [yr yi] = [xr xi] . [[C, -S], [S, C]]        (real form of the DFT-16 matrix)
 // in split TF32x3: x = xh + xl, M = Mh + Ml, y ~= xh.Mh + xh.Ml + xl.Mh with FP32
-// accumulation. One stage is 2 M-tiles (128 instances) x 4 K-steps (K = 8 TF32) x 3
-// products = 24 MMAs (kind::tf32, M = 128, N = 32) into 64 TMEM columns; each thread
-// reads its 32 results back with tcgen05.ld.32x32b, applies the FP32 twiddle
-// W256^(n1 k2) and scatters them into the next stage's A rows.
+// accumulation. One stage is P / 8 M-tiles (128 instances) x 4 K-steps (K = 8 TF32) x 3
+// products = 12 MMAs per M-tile (kind::tf32, M = 128, N = 32) into 32 TMEM columns per
+// M-tile; each thread reads its 32 results back with tcgen05.ld.32x32b, applies the
+// FP32 twiddle W256^(n1 k2) and scatters them into the next stage's A rows.
 //
-// Operand layouts (K-major, TF32), SW = 0: canonical layout without swizzle (8-row x
-// 16-byte core matrices, 128 bytes apart along K, 1024 bytes between 8-row groups);
-// SW = 1: 128-byte swizzle (one 8 x 128-byte atom per 8-row group, 16-byte chunk c of
-// row r stored at chunk c ^ r), which spreads the stage-2 scatter over more banks.
+// Operand layout (K-major, TF32, 128-byte swizzle): one 8-row x 128-byte atom per
+// 8-row group (1024 bytes apart), 16-byte chunk c of row r stored at chunk c ^ (r & 7);
+// the K-step s descriptor starts 32 s bytes into the atom.
 //
-// Pencil mapping (instance (a, b) = thread 16 a + b; stage-1 input n2, stage-2 output k1):
-//   strided tile (256 positions x 16 columns): a = n1 or k2, b = column;
-//     stage-1 inputs at positions a + 16 n2, stage-2 outputs at positions a + 16 k1.
-//   row tile (16 rows x 256): a = row, b = n1 or k2; the same positions along row a.
-// The fused z ops keep the forward spectrum in registers: the thread that ends the
-// forward transform with positions k2 + 16 k1 of column c owns the inverse's stage-1
-// instance (n1 = k2, c), so multiply and inverse continue without a round trip.
+// Pencil mapping (stage-1 input n2, stage-2 output k1):
+//   strided tile (256 positions x P columns): thread m = P a + b, a = n1 or k2, b = column;
+//     stage-1 inputs at positions a + 16 n2, stage-2 outputs at positions a + 16 k1;
+//     stage-2 instance (k2, b) is row P k2 + b (the scatter is bank-conflict free for P = 8).
+//   row tile (P rows x 256): thread m = 16 a + b, a = row, b = n1 or k2; the same
+//     positions along row a; stage-2 instance (a, k2) is row 16 a + k2.
+// The fused z ops continue from registers: the thread that ends the forward transform
+// with positions k2 + 16 k1 of column c owns the inverse's stage-1 instance (n1 = k2, c).
+// The operand that waits while another is transformed (the signal during the filter's
+// transform, the filter spectrum during the signal's) is parked in spare TMEM columns.
 //
-// Shared memory (from a 1024-byte aligned base): A hi (aliases the TMA tile), A lo
-// (aliases the filter tile), B hi, B lo, twiddles, barriers. The tiles are read into
-// registers before the first A row is written.
+// Shared memory (1024-byte aligned base): A hi (aliases the signal tile), A lo (aliases
+// the filter tile), B hi, B lo, twiddles W256^j (one bulk copy of a constant block built
+// once per device by k_tc05_consts), barriers. The tiles are read into registers before
+// the first A row is written.
 //
 // Ordering: a stage's MMAs are issued after a barrier that every thread reaches only
 // after its previous tcgen05.ld completed (tcgen05.fence::before_thread_sync before it,
@@ -42,36 +45,38 @@ namespace convgpu {
 constexpr unsigned kStatusMmaTimeout = 4u;  // a tcgen05 completion wait gave up
 constexpr unsigned kStatusSmemAlign = 8u;   // dynamic shared memory not 1024-byte aligned
 
-constexpr int kT5Threads = 256;
-constexpr int kT5ABytes = 256 * 32 * 4;  // one A part (hi or lo): 256 rows x 32 TF32
-constexpr int kT5BBytes = 32 * 32 * 4;   // one B part: 32 x 32 TF32
-constexpr int kT5OffB = 2 * kT5ABytes;
-constexpr int kT5OffTw = kT5OffB + 2 * kT5BBytes;
-constexpr int kT5OffBar = kT5OffTw + 256 * 8;
-constexpr int kT5Smem = kT5OffBar + 128;
-constexpr uint32_t kT5Sbo = 1024;
+// Constant block (bytes): B hi | B lo | W256^j, j < 256. It sits in the twiddle buffer
+// handed to the tensor-core path, right after the 512 twiddles W512^j.
+constexpr int kT5BBytes = 32 * 32 * 4;  // one B part: 32 x 32 TF32
+constexpr int kT5ConstBytes = 2 * kT5BBytes + 256 * 8;
+constexpr int kT5ConstOffset = 512 * 8;
+
+template <int P>
+struct T5Geom {
+  static_assert(P == 8 || P == 16, "8 or 16 pencils per CTA");
+  static constexpr int kThreads = 16 * P;
+  static constexpr int kMTiles = P / 8;
+  static constexpr int kABytes = 16 * P * 128;  // one A part: 16 P rows x 32 TF32
+  static constexpr int kOffB = 2 * kABytes;
+  static constexpr int kOffTw = kOffB + 2 * kT5BBytes;
+  static constexpr int kOffBar = kOffB + kT5ConstBytes;
+  static constexpr int kSmem = kOffBar + 128;
+  static constexpr int kMinBlocks = P == 8 ? 5 : 3;
+};
+
 // kind::tf32, D F32, A / B TF32 K-major, N = 32, M = 128
 constexpr uint32_t kT5Idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((32u >> 3) << 17) | ((128u >> 4) << 24);
 
-template <int SW>
+// Shared-memory descriptor: start address, LBO 16 (unused by swizzled K-major), SBO 1024,
+// version 1 (bit 46), 128-byte swizzle (layout type 2, bits 61-63).
 __device__ __forceinline__ uint64_t t5_desc(uint32_t addr) {
-  constexpr uint32_t lbo = SW ? 16u : 128u;
-  constexpr uint64_t layout = SW ? 2ull : 0ull;  // 2 = 128-byte swizzle
-  return (uint64_t)((addr >> 4) & 0x3FFF) | ((uint64_t)((lbo >> 4) & 0x3FFF) << 16) |
-         ((uint64_t)((kT5Sbo >> 4) & 0x3FFF) << 32) | (1ull << 46) | (layout << 61);
-}
-
-// Byte offset of the start of K-step s (8 TF32) inside an operand.
-template <int SW>
-__device__ __forceinline__ uint32_t t5_kstep(int s) {
-  return SW ? (uint32_t)(32 * s) : (uint32_t)(256 * s);
+  return (uint64_t)((addr >> 4) & 0x3FFF) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) | (1ull << 46) |
+         (2ull << 61);
 }
 
 // Byte offset of element (row m, k) of a K-major TF32 operand (32 K values per row).
-template <int SW>
 __device__ __forceinline__ uint32_t t5_off(int m, int k) {
-  if (SW) return (uint32_t)((m >> 3) * 1024 + (m & 7) * 128 + ((((k >> 2) ^ (m & 7)) & 7) << 4) + (k & 3) * 4);
-  return (uint32_t)((m >> 3) * 1024 + (k >> 2) * 128 + (m & 7) * 16 + (k & 3) * 4);
+  return (uint32_t)((m >> 3) * 1024 + (m & 7) * 128 + ((((k >> 2) ^ m) & 7) << 4) + (k & 3) * 4);
 }
 
 __device__ __forceinline__ uint32_t t5_rna(float x) {
@@ -83,18 +88,43 @@ __device__ __forceinline__ uint32_t t5_rna(float x) {
 __device__ __forceinline__ void t5_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void t5_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
+// One-block kernel writing the constant block: B[o][k] with o = output (re k2, then im
+// k2), k = input (re n2, then im n2); W16^(k2 n2) = (c, -s) gives re = xr c + xi s,
+// im = -xr s + xi c. Split into TF32 hi and lo parts in the swizzled layout.
+__global__ void k_tc05_consts(unsigned char *blk, const float2 *tw512) {
+  for (int i = threadIdx.x; i < 32 * 32; i += blockDim.x) {
+    const int o = i >> 5, k = i & 31;
+    const float2 w = tw512[32 * (((o & 15) * (k & 15)) & 15)];
+    const float c = w.x, s = -w.y;
+    const float v = o >= 16 ? (k >= 16 ? c : -s) : (k >= 16 ? s : c);
+    const uint32_t h = t5_rna(v);
+    const uint32_t off = t5_off(o, k);
+    *reinterpret_cast<uint32_t *>(blk + off) = h;
+    *reinterpret_cast<uint32_t *>(blk + kT5BBytes + off) = t5_rna(v - __uint_as_float(h));
+  }
+  float2 *tw = reinterpret_cast<float2 *>(blk + 2 * kT5BBytes);
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) tw[i] = tw512[2 * i];
+}
+
+__device__ __forceinline__ void bulk_load(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+               "l"(reinterpret_cast<uint64_t>(src)), "r"(bytes), "r"(bar)
+               : "memory");
+}
+
+template <int P>
 struct T5Ctx {
   unsigned char *ah, *al;  // A operand parts (hi, lo)
   uint32_t bh, bl;         // B operand parts (shared-memory addresses)
-  uint32_t tmem;           // TMEM base (64 columns)
+  uint32_t tmem;           // TMEM base: accumulators at 32 mt, park area after them
   uint32_t bar;            // MMA-completion mbarrier
   uint32_t phase;
   int ok;  // 0 once a completion wait gave up
 };
 
 // Writes thread m's A row from 16 complex inputs (TF32 hi / lo split).
-template <int SW>
-__device__ __forceinline__ void t5_put_row(const T5Ctx &cx, int m, const float2 (&x)[16]) {
+template <int P>
+__device__ __forceinline__ void t5_put_row(const T5Ctx<P> &cx, int m, const float2 (&x)[16]) {
 #pragma unroll
   for (int kg = 0; kg < 8; ++kg) {  // one 16-byte chunk = 4 K values
     uint32_t h[4], l[4];
@@ -105,24 +135,70 @@ __device__ __forceinline__ void t5_put_row(const T5Ctx &cx, int m, const float2 
       h[j] = t5_rna(v);
       l[j] = t5_rna(v - __uint_as_float(h[j]));
     }
-    const uint32_t off = t5_off<SW>(m, kg * 4);
+    const uint32_t off = t5_off(m, kg * 4);
     *reinterpret_cast<uint4 *>(cx.ah + off) = make_uint4(h[0], h[1], h[2], h[3]);
     *reinterpret_cast<uint4 *>(cx.al + off) = make_uint4(l[0], l[1], l[2], l[3]);
   }
 }
 
-template <int SW>
-__device__ __forceinline__ void t5_put(const T5Ctx &cx, int m, int k, float v) {
+template <int P>
+__device__ __forceinline__ void t5_put(const T5Ctx<P> &cx, uint32_t off, float v) {
   const uint32_t h = t5_rna(v);
-  const uint32_t off = t5_off<SW>(m, k);
   *reinterpret_cast<uint32_t *>(cx.ah + off) = h;
   *reinterpret_cast<uint32_t *>(cx.al + off) = t5_rna(v - __uint_as_float(h));
 }
 
-// Runs the 24 MMAs of one stage over the A rows all threads have written and returns
-// this thread's row of D: y[k] = (re out k, im out k).
-template <int SW>
-__device__ __forceinline__ void t5_mma_stage(T5Ctx &cx, float2 (&y)[16]) {
+__device__ __forceinline__ void t5_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+// TMEM address of this warp's 32 lanes in column block `col`.
+__device__ __forceinline__ uint32_t t5_lane_addr(uint32_t tmem, int col) {
+  const int w = threadIdx.x >> 5;
+  return tmem + ((uint32_t)(32 * (w & 3)) << 16) + (uint32_t)(col + 32 * (w >> 2));
+}
+
+// Parks 16 complex values of this thread in the TMEM columns after the accumulators and
+// brings them back: frees 32 registers across a transform.
+template <int P>
+__device__ __forceinline__ void t5_stash_st(const T5Ctx<P> &cx, const float2 (&v)[16]) {
+  uint32_t r[32];
+#pragma unroll
+  for (int k = 0; k < 16; ++k) {
+    r[2 * k] = __float_as_uint(v[k].x);
+    r[2 * k + 1] = __float_as_uint(v[k].y);
+  }
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,"
+      "%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32};" ::"r"(t5_lane_addr(cx.tmem, 32 * (P / 8))),
+      "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]), "r"(r[8]),
+      "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15]), "r"(r[16]),
+      "r"(r[17]), "r"(r[18]), "r"(r[19]), "r"(r[20]), "r"(r[21]), "r"(r[22]), "r"(r[23]), "r"(r[24]),
+      "r"(r[25]), "r"(r[26]), "r"(r[27]), "r"(r[28]), "r"(r[29]), "r"(r[30]), "r"(r[31])
+      : "memory");
+  asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+}
+
+template <int P>
+__device__ __forceinline__ void t5_stash_ld(const T5Ctx<P> &cx, float2 (&v)[16]) {
+  uint32_t r[32];
+  t5_ld32(t5_lane_addr(cx.tmem, 32 * (P / 8)), r);
+#pragma unroll
+  for (int k = 0; k < 16; ++k) v[k] = make_float2(__uint_as_float(r[2 * k]), __uint_as_float(r[2 * k + 1]));
+}
+
+// Runs the MMAs of one stage over the A rows all threads have written and returns this
+// thread's row of D: y[k] = (re out k, im out k).
+template <int P>
+__device__ __forceinline__ void t5_mma_stage(T5Ctx<P> &cx, float2 (&y)[16]) {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   t5_fence_before();
   __syncthreads();
@@ -130,13 +206,13 @@ __device__ __forceinline__ void t5_mma_stage(T5Ctx &cx, float2 (&y)[16]) {
   if (threadIdx.x == 0) {
     const uint32_t ah = smem_u32(cx.ah), al = smem_u32(cx.al);
 #pragma unroll
-    for (int mt = 0; mt < 2; ++mt) {
+    for (int mt = 0; mt < P / 8; ++mt) {
       const uint32_t d = cx.tmem + (uint32_t)(32 * mt);
 #pragma unroll
       for (int s = 0; s < 4; ++s) {
-        const uint32_t ao = (uint32_t)(mt * 16 * 1024) + t5_kstep<SW>(s), bo = t5_kstep<SW>(s);
-        const uint64_t ad[3] = {t5_desc<SW>(ah + ao), t5_desc<SW>(ah + ao), t5_desc<SW>(al + ao)};
-        const uint64_t bd[3] = {t5_desc<SW>(cx.bh + bo), t5_desc<SW>(cx.bl + bo), t5_desc<SW>(cx.bh + bo)};
+        const uint32_t ao = (uint32_t)(mt * 16 * 1024 + 32 * s), bo = (uint32_t)(32 * s);
+        const uint64_t ad[3] = {t5_desc(ah + ao), t5_desc(ah + ao), t5_desc(al + ao)};
+        const uint64_t bd[3] = {t5_desc(cx.bh + bo), t5_desc(cx.bl + bo), t5_desc(cx.bh + bo)};
 #pragma unroll
         for (int q = 0; q < 3; ++q) {
           const uint32_t acc = (s == 0 && q == 0) ? 0u : 1u;
@@ -153,122 +229,72 @@ __device__ __forceinline__ void t5_mma_stage(T5Ctx &cx, float2 (&y)[16]) {
   if (!mbar_wait_bounded(cx.bar, cx.phase)) cx.ok = 0;
   cx.phase ^= 1u;
   t5_fence_after();
-  const int w = threadIdx.x >> 5;
-  const uint32_t taddr = cx.tmem + ((uint32_t)(32 * (w & 3)) << 16) + (uint32_t)(32 * (w >> 2));
   uint32_t r[32];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
-        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
-        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+  t5_ld32(t5_lane_addr(cx.tmem, 0), r);
 #pragma unroll
   for (int k = 0; k < 16; ++k) y[k] = make_float2(__uint_as_float(r[k]), __uint_as_float(r[16 + k]));
 }
 
-// Parks 16 complex values of this thread in TMEM columns 64.. (outside the MMA
-// accumulators) and brings them back: frees 32 registers across a transform.
-__device__ __forceinline__ uint32_t t5_stash_addr(const T5Ctx &cx) {
-  const int w = threadIdx.x >> 5;
-  return cx.tmem + ((uint32_t)(32 * (w & 3)) << 16) + (uint32_t)(64 + 32 * (w >> 2));
-}
-
-__device__ __forceinline__ void t5_stash_st(const T5Ctx &cx, const float2 (&v)[16]) {
-  uint32_t r[32];
-#pragma unroll
-  for (int k = 0; k < 16; ++k) {
-    r[2 * k] = __float_as_uint(v[k].x);
-    r[2 * k + 1] = __float_as_uint(v[k].y);
-  }
-  asm volatile(
-      "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,"
-      "%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32};" ::"r"(t5_stash_addr(cx)),
-      "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]), "r"(r[8]),
-      "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15]), "r"(r[16]),
-      "r"(r[17]), "r"(r[18]), "r"(r[19]), "r"(r[20]), "r"(r[21]), "r"(r[22]), "r"(r[23]), "r"(r[24]),
-      "r"(r[25]), "r"(r[26]), "r"(r[27]), "r"(r[28]), "r"(r[29]), "r"(r[30]), "r"(r[31])
-      : "memory");
-  asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
-}
-
-__device__ __forceinline__ void t5_stash_ld(const T5Ctx &cx, float2 (&v)[16]) {
-  uint32_t r[32];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
-        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
-        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-      : "r"(t5_stash_addr(cx)));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int k = 0; k < 16; ++k) v[k] = make_float2(__uint_as_float(r[2 * k]), __uint_as_float(r[2 * k + 1]));
-}
-
-// 256-point forward transform of the CTA's 16 pencils. On entry x holds thread
-// (a, b)'s stage-1 inputs; on exit its stage-2 outputs (see the mapping above).
-template <int SW, bool ROWS>
-__device__ __forceinline__ void t5_fft256(T5Ctx &cx, float2 (&x)[16], const float2 *tw) {
-  const int m = threadIdx.x, a = m >> 4, b = m & 15;
-  t5_put_row<SW>(cx, m, x);
+// 256-point forward transform of the CTA's P pencils. On entry x holds this thread's
+// stage-1 inputs; on exit its stage-2 outputs (see the mapping above).
+template <int P, bool ROWS>
+__device__ __forceinline__ void t5_fft256(T5Ctx<P> &cx, float2 (&x)[16], const float2 *tw) {
+  const int m = threadIdx.x;
+  const int a = ROWS ? (m >> 4) : (m / P), b = ROWS ? (m & 15) : (m % P);
+  t5_put_row<P>(cx, m, x);
   float2 y[16];
-  t5_mma_stage<SW>(cx, y);
+  t5_mma_stage<P>(cx, y);
   const int n1 = ROWS ? b : a;
+  // stage-2 row m2(k2) and its byte offsets for inputs n1 (re) and 16 + n1 (im)
 #pragma unroll
   for (int k2 = 0; k2 < 16; ++k2) {
     const float2 v = cmul(y[k2], tw[(n1 * k2) & 255]);
-    const int m2 = ROWS ? (16 * a + k2) : (16 * k2 + b);
-    t5_put<SW>(cx, m2, n1, v.x);
-    t5_put<SW>(cx, m2, 16 + n1, v.y);
+    const int m2 = ROWS ? (16 * a + k2) : (P * k2 + b);
+    t5_put<P>(cx, t5_off(m2, n1), v.x);
+    t5_put<P>(cx, t5_off(m2, 16 + n1), v.y);
   }
-  t5_mma_stage<SW>(cx, x);
+  t5_mma_stage<P>(cx, x);
 }
 
-// y / z pass (axis 1 / 2, tile 256 positions x 16 columns) or x pass (ROWS, tile of
-// 16 rows x 256) of 256^3 cubes on tcgen05, with the same tensor maps, grids and
-// output addressing as the FP32 kernels k_strided_tma<256, 16, 16> / k_rows_tma.
-template <int SW, int OP, bool ROWS>
-__global__ void __launch_bounds__(kT5Threads, 3) k_tc05_256(const __grid_constant__ CUtensorMap msrc,
-                                                         const __grid_constant__ CUtensorMap mfilt, PassArgs a,
-                                                         int axis) {
-  constexpr int N = 256, TILE = 4096;
+// y / z pass (axis 1 / 2, tile of 256 positions x P columns) or x pass (ROWS, tile of
+// P rows x 256) of 256^3 cubes on tcgen05. a.tw512 carries the constant block at
+// kT5ConstOffset bytes.
+template <int P, int OP, bool ROWS>
+__global__ void __launch_bounds__(T5Geom<P>::kThreads, T5Geom<P>::kMinBlocks)
+    k_tc05_256(const __grid_constant__ CUtensorMap msrc, const __grid_constant__ CUtensorMap mfilt, PassArgs a,
+               int axis) {
+  using G = T5Geom<P>;
+  constexpr int N = 256, TILE = 256 * P;
   constexpr bool HAS_F = (OP == OP_CONV || OP == OP_CONV_FZ);
-  constexpr int kCols = HAS_F ? 128 : 64;  // accumulators (+ a park area for the fused ops)
+  // accumulators (32 columns per M-tile) + a park area for the fused ops; power of 2 >= 32
+  constexpr uint32_t kCols = HAS_F ? 64u * (P / 8) : 32u * (P / 8);
   static_assert(!(ROWS && HAS_F), "fused ops are z passes");
   extern __shared__ __align__(1024) unsigned char smraw[];
-  if (smem_u32(smraw) & 1023u) {  // the swizzle atoms and descriptors assume this
+  if (smem_u32(smraw) & 1023u) {  // the swizzle atoms assume this
     if (threadIdx.x == 0 && a.status) atomicOr(a.status, kStatusSmemAlign);
     return;
   }
   float2 *tile = reinterpret_cast<float2 *>(smraw);
-  float2 *ftile = tile + TILE;
-  float2 *tw = reinterpret_cast<float2 *>(smraw + kT5OffTw);
-  unsigned char *bbuf = smraw + kT5OffB;
-  const uint32_t tbar = smem_u32(smraw + kT5OffBar), mbar = tbar + 8;
-  uint32_t *tslot = reinterpret_cast<uint32_t *>(smraw + kT5OffBar + 16);
+  float2 *ftile = reinterpret_cast<float2 *>(smraw + G::kABytes);
+  const float2 *tw = reinterpret_cast<const float2 *>(smraw + G::kOffTw);
+  const uint32_t tbar = smem_u32(smraw + G::kOffBar), mbar = tbar + 8;
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(smraw + G::kOffBar + 16);
 
   int vol = 0, row = 0, x0 = 0;
   long long row0 = 0;
   if (ROWS) {
-    row0 = (long long)blockIdx.x * 16;
+    row0 = (long long)blockIdx.x * P;
   } else {
     vol = blockIdx.x / a.groups_per_vol;
     const int rr = blockIdx.x % a.groups_per_vol;
     row = rr / a.groups_x;
-    x0 = (rr % a.groups_x) * 16;
+    x0 = (rr % a.groups_x) * P;
   }
   if (threadIdx.x == 0) {
     mbar_init(tbar, 1);
     mbar_init(mbar, 1);
     mbar_fence_init();
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    mbar_arrive_expect_tx(tbar, (HAS_F ? 2u : 1u) * TILE * 8u);
+    mbar_arrive_expect_tx(tbar, (HAS_F ? 2u : 1u) * TILE * 8u + (uint32_t)kT5ConstBytes);
     if (ROWS) {
       tma_load_2d(smem_u32(tile), &msrc, 0, (int)row0, tbar);
     } else {
@@ -278,51 +304,44 @@ __global__ void __launch_bounds__(kT5Threads, 3) k_tc05_256(const __grid_constan
         tma_load_3d(smem_u32(tile), &msrc, x0, row, vol * N, tbar);
       if constexpr (HAS_F) tma_load_3d(smem_u32(ftile), &mfilt, x0, row, (a.filt_vol_elems ? vol : 0) * N, tbar);
     }
+    bulk_load(smem_u32(smraw + G::kOffB), reinterpret_cast<const unsigned char *>(a.tw512) + kT5ConstOffset,
+              (uint32_t)kT5ConstBytes, tbar);
   }
-  // Twiddles and the DFT-16 matrix while the tile loads. B[o][k]: o = output (re k2,
-  // then im k2), k = input (re n2, then im n2); W16^(k2 n2) = (c, -s) gives
-  // re = xr c + xi s, im = -xr s + xi c.
-  for (int i = threadIdx.x; i < N; i += kT5Threads) tw[i] = a.tw512[2 * i];
-  for (int i = threadIdx.x; i < 32 * 32; i += kT5Threads) {
-    const int o = i >> 5, k = i & 31;
-    const float2 w = a.tw512[32 * (((o & 15) * (k & 15)) & 15)];
-    const float c = w.x, s = -w.y;
-    const float v = o >= 16 ? (k >= 16 ? c : -s) : (k >= 16 ? s : c);
-    const uint32_t h = t5_rna(v);
-    const uint32_t off = t5_off<SW>(o, k);
-    *reinterpret_cast<uint32_t *>(bbuf + off) = h;
-    *reinterpret_cast<uint32_t *>(bbuf + kT5BBytes + off) = t5_rna(v - __uint_as_float(h));
-  }
-  const int loaded = __syncthreads_and(mbar_wait_bounded(tbar, 0) ? 1 : 0);
-  if (!loaded) {  // no TMEM is held yet
-    if (threadIdx.x == 0 && a.status) atomicOr(a.status, kStatusTmaTimeout);
-    mbar_wait_bounded(tbar, 0);
-    return;
-  }
-
-  T5Ctx cx;
-  cx.ah = smraw;
-  cx.al = smraw + kT5ABytes;
-  cx.bh = smem_u32(bbuf);
-  cx.bl = cx.bh + kT5BBytes;
-  cx.bar = mbar;
-  cx.phase = 0;
-  cx.ok = 1;
   if (threadIdx.x < 32) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)),
                  "n"(kCols));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   t5_fence_before();
-  __syncthreads();  // TMEM address published
+  __syncthreads();  // barrier initialised, TMEM address published
   t5_fence_after();
+  T5Ctx<P> cx;
+  cx.ah = smraw;
+  cx.al = smraw + G::kABytes;
+  cx.bh = smem_u32(smraw + G::kOffB);
+  cx.bl = cx.bh + kT5BBytes;
   cx.tmem = *tslot;
+  cx.bar = mbar;
+  cx.phase = 0;
+  cx.ok = 1;
 
-  const int m = threadIdx.x, ia = m >> 4, ib = m & 15;
+  const int loaded = __syncthreads_and(mbar_wait_bounded(tbar, 0) ? 1 : 0);
+  if (!loaded) {
+    if (threadIdx.x == 0 && a.status) atomicOr(a.status, kStatusTmaTimeout);
+    mbar_wait_bounded(tbar, 0);  // copies still in flight land before the CTA exits
+    t5_fence_before();
+    __syncthreads();
+    t5_fence_after();
+    if (threadIdx.x < 32) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(cx.tmem), "n"(kCols));
+    return;
+  }
+
+  const int m = threadIdx.x;
+  const int ia = ROWS ? (m >> 4) : (m / P), ib = ROWS ? (m & 15) : (m % P);
   auto gather = [&](const float2 *t, float2 (&x)[16], bool swap) {
 #pragma unroll
     for (int n2 = 0; n2 < 16; ++n2) {
-      const float2 v = ROWS ? t[ia * N + ib + 16 * n2] : t[(ia + 16 * n2) * 16 + ib];
+      const float2 v = ROWS ? t[ia * N + ib + 16 * n2] : t[(ia + 16 * n2) * P + ib];
       x[n2] = swap ? cswap(v) : v;
     }
   };
@@ -330,7 +349,7 @@ __global__ void __launch_bounds__(kT5Threads, 3) k_tc05_256(const __grid_constan
   if constexpr (OP == OP_FWD || OP == OP_INV) {
     gather(tile, x, OP == OP_INV);
     __syncthreads();  // tile consumed before A (which aliases it) is written
-    t5_fft256<SW, ROWS>(cx, x, tw);
+    t5_fft256<P, ROWS>(cx, x, tw);
     if (OP == OP_INV) {
 #pragma unroll
       for (int k = 0; k < 16; ++k) x[k] = cswap(x[k]);
@@ -338,27 +357,25 @@ __global__ void __launch_bounds__(kT5Threads, 3) k_tc05_256(const __grid_constan
   } else {
     float2 f[16];
     if constexpr (OP == OP_CONV_FZ) {
-      // signal parked in TMEM while the filter is transformed
       gather(tile, x, false);
-      t5_stash_st(cx, x);
+      t5_stash_st<P>(cx, x);  // signal parked while the filter is transformed
       gather(ftile, f, false);
       __syncthreads();
-      t5_fft256<SW, false>(cx, f, tw);
-      t5_stash_ld(cx, x);
-      t5_stash_st(cx, f);
+      t5_fft256<P, false>(cx, f, tw);
+      t5_stash_ld<P>(cx, x);
+      t5_stash_st<P>(cx, f);
     } else {
-      // filter spectrum (positions ia + 16 k1 of column ib) parked in TMEM
 #pragma unroll
-      for (int k1 = 0; k1 < 16; ++k1) f[k1] = ftile[(ia + 16 * k1) * 16 + ib];
-      t5_stash_st(cx, f);
+      for (int k1 = 0; k1 < 16; ++k1) f[k1] = ftile[(ia + 16 * k1) * P + ib];
+      t5_stash_st<P>(cx, f);  // filter spectrum parked
       gather(tile, x, false);
       __syncthreads();
     }
-    t5_fft256<SW, false>(cx, x, tw);
-    t5_stash_ld(cx, f);
+    t5_fft256<P, false>(cx, x, tw);
+    t5_stash_ld<P>(cx, f);
 #pragma unroll
     for (int k1 = 0; k1 < 16; ++k1) x[k1] = cswap(cmul(x[k1], f[k1]));
-    t5_fft256<SW, false>(cx, x, tw);
+    t5_fft256<P, false>(cx, x, tw);
 #pragma unroll
     for (int k = 0; k < 16; ++k) x[k] = cswap(x[k]);
   }
