@@ -177,8 +177,6 @@ static int setup_locked(int dev, bool use_svm) {
   }
   const char *no_tma = std::getenv("CONVGPU_DISABLE_TMA");
   set_tma_enabled(!(no_tma && no_tma[0] == '1'));
-  const char *tc05_p = std::getenv("CONVGPU_TC05_PENCILS");
-  set_tc05_pencils(tc05_p ? std::atoi(tc05_p) : 8);
   g.device = dev;
   g.use_svm = use_svm;
   g.init = true;

@@ -32,9 +32,6 @@ cudaError_t launch_axis_pass_tc(int n, int axis, int op, const float2 *src, floa
 // Selects the TMA-fed y / z pass kernels (default) or the register-gather kernels.
 void set_tma_enabled(bool on);
 
-// Pencils per CTA of the tcgen05 kernels (8 default, or 16).
-void set_tc05_pencils(int p);
-
 // Twiddle buffer of the engine: 512 twiddles W512^j followed by the constant block of
 // the tcgen05 kernels (B operand hi / lo, W256^j), written by tc05_init_consts.
 constexpr size_t kTwiddleBufBytes = 512 * 8 + 2 * 4096 + 256 * 8;

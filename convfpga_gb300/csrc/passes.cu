@@ -127,8 +127,6 @@ unsigned int read_and_clear_device_status() {
 // ------------------------------------------------------------------ plan table
 static bool g_use_tma = true;
 void set_tma_enabled(bool on) { g_use_tma = on; }
-static int g_tc05_pencils = 8;
-void set_tc05_pencils(int p) { g_tc05_pencils = p == 16 ? 16 : 8; }
 
 static std::atomic<int> g_variant[6][kPassKinds];
 
@@ -280,7 +278,7 @@ cudaError_t launch_axis_pass_tc(int n, int axis, int op, const float2 *src, floa
   // split TF32: tcgen05 kernels (plan kind kKindTc, variant 0) or mma.sync (variant 1);
   // BF16x3: mma.sync
   const cudaError_t e = (prec == kTcTf32x3 && get_pass_variant(n, kKindTc) == 0)
-                            ? launch_tc05_entry(r, g_tc05_pencils)
+                            ? launch_tc05_entry(r)
                             : launch_tc256_entry(r, prec == kTcBf16x3 ? 1 : 0);
   if (e == cudaErrorNotSupported)
     return launch_axis_pass(n, axis, op, src, dst, filt, filt_vol_elems, nvol, scale, tw512, s);

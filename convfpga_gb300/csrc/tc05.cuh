@@ -5,9 +5,12 @@
 // A 256-point transform is 16 x 16 (four-step). A CTA holds P pencils (P = 8 or 16),
 // i.e. 16 P instances of each 16-point stage; thread m owns instance m and its A row
 //   [yr yi] = [xr xi] . [[C, -S], [S, C]]        (real form of the DFT-16 matrix)
-// in split TF32x3: x = xh + xl, M = Mh + Ml, y ~= xh.Mh + xh.Ml + xl.Mh with FP32
-// accumulation. One stage is P / 8 M-tiles (128 instances) x 4 K-steps (K = 8 TF32) x 3
-// products = 12 MMAs per M-tile (kind::tf32, M = 128, N = 32) into 32 TMEM columns per
+// in split TF32x3: x = xh + xl, M = Mh + Ml, y ~= xh.Ml + xl.Mh + xh.Mh with FP32
+// accumulation, the two small products first so that they add up at their own scale.
+// xh is x rounded to TF32 (nearest, ties away: add half an ulp to the bit pattern, clear
+// the 13 low bits), xl = x - xh truncated to TF32; both are exact TF32 bit patterns
+// made with integer operations only. One stage is P / 8 M-tiles (128 instances) x 4
+// K-steps (K = 8 TF32) x 3 products = 12 MMAs per M-tile (kind::tf32, M = 128, N = 32) into 32 TMEM columns per
 // M-tile; each thread reads its 32 results back with tcgen05.ld.32x32b, applies the
 // FP32 twiddle W256^(n1 k2) and scatters them into the next stage's A rows.
 //
@@ -85,6 +88,12 @@ __device__ __forceinline__ uint32_t t5_rna(float x) {
   return r;
 }
 
+// Operand split of a data value: (TF32 nearest of v, TF32 truncation of the rest).
+__device__ __forceinline__ uint2 t5_split(float v) {
+  const uint32_t h = (__float_as_uint(v) + 0x1000u) & 0xFFFFE000u;
+  return make_uint2(h, __float_as_uint(v - __uint_as_float(h)) & 0xFFFFE000u);
+}
+
 __device__ __forceinline__ void t5_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void t5_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
@@ -131,9 +140,9 @@ __device__ __forceinline__ void t5_put_row(const T5Ctx<P> &cx, int m, const floa
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const int k = kg * 4 + j;
-      const float v = k < 16 ? x[k].x : x[k - 16].y;
-      h[j] = t5_rna(v);
-      l[j] = t5_rna(v - __uint_as_float(h[j]));
+      const uint2 hl = t5_split(k < 16 ? x[k].x : x[k - 16].y);
+      h[j] = hl.x;
+      l[j] = hl.y;
     }
     const uint32_t off = t5_off(m, kg * 4);
     *reinterpret_cast<uint4 *>(cx.ah + off) = make_uint4(h[0], h[1], h[2], h[3]);
@@ -143,9 +152,9 @@ __device__ __forceinline__ void t5_put_row(const T5Ctx<P> &cx, int m, const floa
 
 template <int P>
 __device__ __forceinline__ void t5_put(const T5Ctx<P> &cx, uint32_t off, float v) {
-  const uint32_t h = t5_rna(v);
-  *reinterpret_cast<uint32_t *>(cx.ah + off) = h;
-  *reinterpret_cast<uint32_t *>(cx.al + off) = t5_rna(v - __uint_as_float(h));
+  const uint2 hl = t5_split(v);
+  *reinterpret_cast<uint32_t *>(cx.ah + off) = hl.x;
+  *reinterpret_cast<uint32_t *>(cx.al + off) = hl.y;
 }
 
 __device__ __forceinline__ void t5_ld32(uint32_t taddr, uint32_t (&r)[32]) {
@@ -208,18 +217,18 @@ __device__ __forceinline__ void t5_mma_stage(T5Ctx<P> &cx, float2 (&y)[16]) {
 #pragma unroll
     for (int mt = 0; mt < P / 8; ++mt) {
       const uint32_t d = cx.tmem + (uint32_t)(32 * mt);
+      // products xh.Ml, xl.Mh (small) for all K-steps, then xh.Mh
 #pragma unroll
-      for (int s = 0; s < 4; ++s) {
-        const uint32_t ao = (uint32_t)(mt * 16 * 1024 + 32 * s), bo = (uint32_t)(32 * s);
-        const uint64_t ad[3] = {t5_desc(ah + ao), t5_desc(ah + ao), t5_desc(al + ao)};
-        const uint64_t bd[3] = {t5_desc(cx.bh + bo), t5_desc(cx.bl + bo), t5_desc(cx.bh + bo)};
+      for (int q = 0; q < 3; ++q) {
 #pragma unroll
-        for (int q = 0; q < 3; ++q) {
+        for (int s = 0; s < 4; ++s) {
+          const uint32_t ao = (uint32_t)(mt * 16 * 1024 + 32 * s), bo = (uint32_t)(32 * s);
+          const uint32_t aa = (q == 1 ? al : ah) + ao, bb = (q == 0 ? cx.bl : cx.bh) + bo;
           const uint32_t acc = (s == 0 && q == 0) ? 0u : 1u;
           asm volatile(
               "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
               "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d),
-              "l"(ad[q]), "l"(bd[q]), "r"(kT5Idesc), "r"(acc));
+              "l"(t5_desc(aa)), "l"(t5_desc(bb)), "r"(kT5Idesc), "r"(acc));
         }
       }
     }

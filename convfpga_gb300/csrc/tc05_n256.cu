@@ -1,6 +1,6 @@
 // Launchers of the tcgen05 split-TF32 pass kernels for 256^3 cubes (tc05.cuh): the x
-// pass takes P rows per CTA (box {256, P}), the y / z passes P columns x 256 positions
-// per CTA (P = 8 by default, 16 with CONVGPU_TC05_PENCILS=16).
+// pass takes P = 8 rows per CTA (box {256, 8}), the y / z passes 8 columns x 256
+// positions per CTA (5 CTAs per SM).
 #define CONVGPU_PASS_LAUNCH_IMPL
 #include "pass_launch.cuh"
 #include "tc05.cuh"
@@ -59,13 +59,10 @@ static cudaError_t launch_tc05_op(int op, int axis, const PassArgs &a, int nvol,
   }
 }
 
-// tcgen05 pass of a 256^3 batch with `pencils` (8 or 16) per CTA; r.a.tw512 must carry
-// the constant block (tc05_init_consts). cudaErrorNotSupported when tensor maps cannot
-// describe the operands (the caller then runs the FP32 kernels).
-cudaError_t launch_tc05_entry(const PassReq &r, int pencils) {
-  return pencils == 16 ? launch_tc05_op<16>(r.op, r.axis, r.a, r.nvol, r.s)
-                       : launch_tc05_op<8>(r.op, r.axis, r.a, r.nvol, r.s);
-}
+// tcgen05 pass of a 256^3 batch; r.a.tw512 must carry the constant block
+// (tc05_init_consts). cudaErrorNotSupported when tensor maps cannot describe the
+// operands (the caller then runs the FP32 kernels).
+cudaError_t launch_tc05_entry(const PassReq &r) { return launch_tc05_op<8>(r.op, r.axis, r.a, r.nvol, r.s); }
 
 // Writes the tcgen05 constant block behind the 512 twiddles of `tw` (a buffer of at
 // least kTwiddleBufBytes bytes) and waits for it.
