@@ -48,6 +48,9 @@ def _args():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling runs)")
     p.add_argument("--batch", type=int, default=BATCH, help="cubes per step (profiling runs use 1)")
+    p.add_argument("--plan-cache", default=None,
+                   help="plan-cache file: loaded instead of autotuning when it exists, written by the "
+                        "autotuner otherwise (profiling runs replay the plan of the plain run)")
     p.add_argument("--workload", choices=["c256x4", "uneven96"], default="c256x4",
                    help="c256x4: the headline 256^3 x4 workload; uneven96: 96 convolutions of sizes "
                         "32..256 (work-queue launch vs one job at a time)")
@@ -78,7 +81,7 @@ def _config(path: str) -> dict:
         "n": N,
         "batch": BATCH,
         "filters": "per-signal",
-        "path": {"fp32": "plain FP32 per-axis passes", "tc": "tensor-core BF16x3 split"}[path],
+        "path": {"fp32": "plain FP32 per-axis passes", "tc": "tcgen05 split-TF32 (TF32x3) per-axis passes"}[path],
         "normalised": False,
         "l2": "no flush: each step reads 1 GiB of inputs (> 129 MB L2)",
     }
@@ -239,7 +242,8 @@ def run_ours(a) -> None:
         from convfpga_gb300 import build
 
         build.build()
-    rc = cg.fpga_initialize(f"cuda:{local}", "convgpu_plans.json", False)
+    replay = bool(a.plan_cache) and os.path.exists(a.plan_cache)
+    rc = cg.fpga_initialize(f"cuda:{local}", a.plan_cache or "convgpu_plans.json", False)
     if rc != 0:
         raise SystemExit(f"fpga_initialize failed: {rc} {cg.last_error()}")
 
@@ -247,7 +251,8 @@ def run_ours(a) -> None:
     BATCH = a.batch
     # The library's autotuner picks the plan for this size (shape variants, fused x+y
     # pass or not) on this GPU before anything is timed.
-    cg.autotune([N], write_cache=False)
+    if not replay:
+        cg.autotune([N], write_cache=bool(a.plan_cache))
     plan = {k: cg.plan_variant(N, i) for i, k in enumerate(cg.PLAN_KINDS)}
     flags = cg.FILTER_PER_SIGNAL | (cg.TENSOR_SPLIT if a.path == "tc" else 0)
     g = torch.Generator(device="cuda").manual_seed(1234 + rank)
@@ -322,7 +327,7 @@ def run_ours(a) -> None:
     line = {
         "metric": METRIC, "value": value, "unit": "conv/s", "n_gpus": world, "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "bf16x3" if a.path == "tc" else "f32",
+        "vs_baseline": None, "dtype": "tf32x3" if a.path == "tc" else "f32",
         "data": "synthetic (seeded torch generator; signals N(0,1), filters U[-1,1])",
         "config": _config(a.path),
         "hbm_gbs_model": round(model_bytes / (ms_step / 1e3) / 1e9, 1),
