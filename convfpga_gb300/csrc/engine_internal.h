@@ -46,9 +46,11 @@ int pass_kind(int axis, int op);
 void set_pass_variant(int n, int kind, int variant);
 int get_pass_variant(int n, int kind);
 // Fused x + y pass over `nplanes` planes (N = 256 only; cudaErrorNotSupported otherwise
-// or when tensor maps cannot describe the operands). Plan kind kKindXy, variant 1.
+// or when tensor maps cannot describe the operands). Plan kind kKindXy: variant 1 stages
+// the x-transformed planes through an L2-resident scratch ring (one persistent kernel),
+// variant 2 keeps each plane in the shared memory of an 8-CTA cluster.
 cudaError_t launch_xy_pass(int n, const float2 *src, float2 *dst, int nplanes, bool inverse, float scale,
-                           const float2 *tw512, cudaStream_t s);
+                           const float2 *tw512, cudaStream_t s, int variant);
 // x or y pass (FWD / INV) over `nplanes` consecutive N x N planes starting at src / dst
 // (a slab of a cube; planes are independent for these axes).
 cudaError_t launch_axis_pass_planes(int n, int axis, int op, const float2 *src, float2 *dst, int nplanes, float scale,
@@ -74,6 +76,7 @@ cudaError_t launch_axis_pass_table(int n, int axis, int op, const CUtensorMap *m
 int uneven_grouped(const struct UnevenJob *jobs, unsigned njobs, const void *d_sig, const void *d_filt,
                    void *d_out, bool normalize, const float2 *tw512, cudaStream_t stream, std::string &err);
 void release_grouped_plans();
+void release_xy_l2();
 
 // Device address of the status word (for kernels outside passes.cu).
 unsigned int *device_status_address();

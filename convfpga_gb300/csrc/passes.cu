@@ -151,7 +151,8 @@ int pass_kind(int axis, int op) {
 
 void set_pass_variant(int n, int kind, int variant) {
   const int i = size_index(n);
-  if (i >= 0 && kind >= 0 && kind < kPassKinds) g_variant[i][kind].store(variant ? 1 : 0);
+  if (i >= 0 && kind >= 0 && kind < kPassKinds)
+    g_variant[i][kind].store(kind == kKindXy ? (variant < 0 ? 0 : (variant > 2 ? 2 : variant)) : (variant ? 1 : 0));
 }
 
 int get_pass_variant(int n, int kind) {
@@ -286,9 +287,10 @@ cudaError_t launch_axis_pass_tc(int n, int axis, int op, const float2 *src, floa
 }
 
 cudaError_t launch_xy_pass(int n, const float2 *src, float2 *dst, int nplanes, bool inverse, float scale,
-                           const float2 *tw512, cudaStream_t s) {
+                           const float2 *tw512, cudaStream_t s, int variant) {
   if (n != 256 || !g_use_tma) return cudaErrorNotSupported;
-  return launch_xy256(src, dst, nplanes, inverse, scale, tw512, device_status_address(), s);
+  if (variant == 2) return launch_xy256(src, dst, nplanes, inverse, scale, tw512, device_status_address(), s);
+  return launch_xy_l2(src, dst, nplanes, inverse, scale, tw512, device_status_address(), s);
 }
 
 cudaError_t probe_kernel_image() {

@@ -65,6 +65,13 @@ struct RowSlot {  // x pass: pencil-major, one 8-byte pad every 16 slots
 };
 template <int N>
 constexpr int row_pitch() { return N + N / 16; }
+// x pass of N = 256 in an unpadded row: the low 4 bits of the position XOR-swizzled by
+// bits 4..7, which makes the Stockham exchange of a 16 x 16 row transform free of bank
+// conflicts in the row's own N slots (the tile a TMA row load lands in).
+struct SwzRow {
+  int base;
+  __device__ __forceinline__ int operator()(int n) const { return base + (n ^ ((n >> 4) & 15)); }
+};
 
 template <int N, int E, int NS, class SIdx, int R, int... Rest>
 __device__ __forceinline__ void run_stages(float2 (&v)[E], int t, const float2 *tw, float2 *sm, const SIdx &sidx) {

@@ -30,14 +30,6 @@ constexpr int kXyTile = kXyRows * 256;                    // complex values per 
 // Dynamic shared memory: 2 barriers (128 B), two row tiles, the column tile, twiddles.
 constexpr int kXySmem = 128 + 3 * kXyTile * 8 + 256 * 8;
 
-// Row slot with an XOR swizzle of the low 4 bits by bits 4..7 of the position: the
-// Stockham exchange of a 16 x 16 row transform is then free of bank conflicts while
-// the natural (unswizzled) layout is restored when the row is written back.
-struct SwzRow {
-  int base;
-  __device__ __forceinline__ int operator()(int n) const { return base + (n ^ ((n >> 4) & 15)); }
-};
-
 template <bool INV>
 __global__ void __cluster_dims__(kXyCluster, 1, 1) __launch_bounds__(kXyThreads, 1)
     k_xy256(const __grid_constant__ CUtensorMap mrows, float2 *__restrict__ dst, int nplanes, float scale,

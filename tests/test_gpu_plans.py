@@ -65,10 +65,12 @@ def test_512_variants(gpu, restore_plans, variant):
 
 
 @pytest.mark.parametrize("variant", [0, 1])
-def test_fused_xy_pass_256(gpu, restore_plans, variant):
-    """x and y of 256^3 cubes as one pass on 8-CTA clusters (plan kind 4, variant 1),
-    forward and inverse, with shared and per-signal filters, and through the host path."""
-    gpu.plan_variant(256, 4, 1)
+@pytest.mark.parametrize("xy", [1, 2], ids=["l2_staged", "cluster"])
+def test_fused_xy_pass_256(gpu, restore_plans, variant, xy):
+    """x and y of 256^3 cubes as one pass (plan kind 4): variant 1 stages the x-transformed
+    planes through an L2-resident scratch ring, variant 2 holds each plane in an 8-CTA
+    cluster's shared memory. Forward and inverse, shared and per-signal filters, host path."""
+    assert gpu.plan_variant(256, 4, xy) == xy
     for k in range(KINDS):
         gpu.plan_variant(256, k, variant)
     _check(gpu, 256, 2, per_signal=False)
