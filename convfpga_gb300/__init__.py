@@ -37,6 +37,7 @@ TENSOR_BF16X3 = 1 << 4
 UNEVEN_PER_JOB = 1 << 5
 UNEVEN_QUEUE = 1 << 6
 HOST_SLABS = 1 << 7
+FILTER_CACHED = 1 << 8
 
 OK, EINVAL, ENOTINIT, ECUDA, ENOMEM, EUNSUPPORTED = 0, -1, -2, -3, -4, -5
 

@@ -28,6 +28,8 @@ extern "C" {
 #define CONVGPU_UNEVEN_PER_JOB (1u << 5)       /* uneven batch: one job at a time */
 #define CONVGPU_UNEVEN_QUEUE (1u << 6)         /* uneven batch: one persistent work-queue launch */
 #define CONVGPU_HOST_SLABS (1u << 7)           /* host batch: stream cubes >= 32 MiB in z-slabs */
+#define CONVGPU_FILTER_CACHED (1u << 8)        /* host batch: shared filter unchanged since the
+                                                  last call with this flag, same pointer and N */
 
 /* Status codes */
 #define CONVGPU_OK 0
@@ -67,9 +69,15 @@ int convgpu_conv3d_device(unsigned N, const float2 *d_sig, const float2 *d_filte
 int convgpu_conv3d_device_noalloc(unsigned N, const float2 *d_sig, const float2 *d_filter, float2 *d_out,
                                   unsigned how_many, unsigned flags, void *stream);
 
-/* Host-buffer batch with the flags above (CONVGPU_TENSOR_SPLIT and
- * CONVGPU_FILTER_IS_SPECTRUM excluded). Copies overlap compute on separate streams;
- * pinned buffers (convgpu_host_alloc) copy fastest.
+/* Host-buffer batch with the flags above (CONVGPU_FILTER_IS_SPECTRUM excluded). Copies
+ * overlap compute on separate streams; pinned buffers (convgpu_host_alloc) copy fastest.
+ * Filter-spectrum cache: with CONVGPU_FILTER_CACHED and a shared filter, the caller states
+ * that the filter behind this host pointer has not changed since the last call that
+ * passed the same pointer, N and tensor-core flags with CONVGPU_FILTER_CACHED; the library
+ * then reuses the spectrum it kept on the device and neither copies nor transforms the
+ * filter again (fpga_t reports 0 for both filter fields). Any call that does not hit the
+ * cache, and fpga_final, drop the kept spectrum. The reference copies and transforms the
+ * filter on every call (host/src/convfpga.c:74-172).
  * Extends fpgaf_conv3D_svm_batch (host/include/convfpga/convfpga.h:46). */
 fpga_t convgpu_conv3d_host(unsigned N, const float2 *sig, const float2 *filter, float2 *out,
                            unsigned how_many, unsigned flags);

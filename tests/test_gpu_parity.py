@@ -144,6 +144,44 @@ def test_host_batch_chunked_per_signal(gpu):
     assert snr_db(ref, out) > SNR_DB
 
 
+@pytest.mark.parametrize("slabs", [False, True], ids=["whole", "slabs"])
+def test_host_filter_spectrum_cache(gpu, slabs):
+    """CONVGPU_FILTER_CACHED: the second call with the same shared filter pointer reuses the
+    kept spectrum (no filter copy or transform, bit-identical output); a filter changed in
+    place is not seen while the flag promises it is unchanged; a call without the flag
+    transforms it again and drops the kept spectrum."""
+    rng = np.random.default_rng(21)
+    n, b = (256, 2) if slabs else (64, 3)  # the slab pipeline takes cubes of 32 MiB and more
+    extra = gpu.HOST_SLABS if slabs else 0
+    sig = _c64(rng, (b, n, n, n))
+    filt = _c64(rng, (n, n, n))
+    filt2 = _c64(rng, (n, n, n))
+    outs = []
+    times = []
+    for _ in range(2):
+        out = np.zeros_like(sig)
+        t = gpu.conv3d_host(n, sig, filt, out, b, gpu.FILTER_CACHED | extra)
+        assert t.valid, gpu.last_error()
+        outs.append(out)
+        times.append(t)
+    assert snr_db(conv3d(sig, filt, "fp32", engine="pocketfft"), outs[0]) > SNR_DB
+    np.testing.assert_array_equal(outs[0], outs[1])
+    assert times[0].filter_exec_t > 0.0 and times[1].filter_exec_t == 0.0
+    assert times[1].filter_pcie_wr_t == 0.0
+    filt[...] = filt2  # same pointer, new contents: the promise is broken on purpose
+    stale = np.zeros_like(sig)
+    assert gpu.conv3d_host(n, sig, filt, stale, b, gpu.FILTER_CACHED | extra).valid
+    np.testing.assert_array_equal(stale, outs[0])
+    fresh = np.zeros_like(sig)
+    assert gpu.conv3d_host(n, sig, filt, fresh, b, extra).valid  # no flag: transformed again
+    assert snr_db(conv3d(sig, filt2, "fp32", engine="pocketfft"), fresh) > SNR_DB
+    again = np.zeros_like(sig)
+    t = gpu.conv3d_host(n, sig, filt, again, b, gpu.FILTER_CACHED | extra)
+    assert t.valid and t.filter_exec_t > 0.0  # the unflagged call dropped the kept spectrum
+    np.testing.assert_array_equal(again, fresh)
+    assert gpu.device_status() == 0
+
+
 def test_uneven_jobs(gpu):
     rng = np.random.default_rng(9)
     sizes = [32, 64, 16, 128, 32]
