@@ -38,6 +38,7 @@ UNEVEN_PER_JOB = 1 << 5
 UNEVEN_QUEUE = 1 << 6
 HOST_SLABS = 1 << 7
 FILTER_CACHED = 1 << 8
+FILTER_REAL = 1 << 9
 
 OK, EINVAL, ENOTINIT, ECUDA, ENOMEM, EUNSUPPORTED = 0, -1, -2, -3, -4, -5
 
@@ -177,8 +178,9 @@ def _host_ptr(a) -> int | None:
     if isinstance(a, int):
         return a
     if isinstance(a, np.ndarray):
-        if a.dtype != np.complex64 or not a.flags.c_contiguous:
-            raise TypeError("host arrays must be C-contiguous complex64")
+        # complex64; float32 for real filters (FILTER_REAL)
+        if a.dtype not in (np.complex64, np.float32) or not a.flags.c_contiguous:
+            raise TypeError("host arrays must be C-contiguous complex64 (or float32 real filters)")
         return a.ctypes.data
     if hasattr(a, "data_ptr"):  # CPU torch tensor (e.g. pinned)
         return a.data_ptr()

@@ -43,6 +43,7 @@ constexpr unsigned kFlagUnevenPerJob = 1u << 5;
 constexpr unsigned kFlagUnevenQueue = 1u << 6;
 constexpr unsigned kFlagHostSlabs = 1u << 7;
 constexpr unsigned kFlagFilterCached = 1u << 8;
+constexpr unsigned kFlagFilterReal = 1u << 9;
 
 constexpr int kErrInval = -1;
 constexpr int kErrNotInit = -2;
@@ -99,6 +100,7 @@ struct Engine {
   float2 *tw512 = nullptr;
   DevBuf ws;           // device API workspace (filter spectra)
   DevBuf hfilt;        // host API: filter input / spectrum
+  DevBuf hreal[4];     // host API, real filters: float staging (3 chunk buffers + shared filter)
   // Key of the shared-filter spectrum held in hfilt (host API, CONVGPU_FILTER_CACHED):
   // the caller's filter pointer, N and path; valid only until hfilt is used otherwise.
   struct {
@@ -137,6 +139,7 @@ static void teardown_locked() {
   release_xy_l2();
   g.ws.release();
   g.hfilt.release();
+  for (auto &b : g.hreal) b.release();
   g.hkey.valid = false;
   for (auto &b : g.hio) b.release();
   for (auto &b : g.hfio) b.release();
@@ -274,13 +277,35 @@ static bool use_xy(int n, int tc) { return tc == 0 && n == 256 && get_pass_varia
     count_launches(1);                      \
   } while (0)
 
-// Filter spectra of `count` filters (x, y and, unless xy_only, z passes) into spec.
+// x pass of real filter cubes (N^3 floats each) into complex spectra, profiled in the
+// x-fwd slot with its own bytes (4 read + 8 written per point).
+static cudaError_t pass_real(int n, const float *filt, float2 *spec, int count, cudaStream_t s) {
+  PassRec r{0 * 4 + OP_FWD, 0.0, nullptr, nullptr};
+  if (g_prof) {
+    r.bytes = 12.0 * (double)n * n * n * count;
+    cudaEventCreate(&r.a);
+    cudaEventCreate(&r.b);
+    cudaEventRecord(r.a, s);
+  }
+  const cudaError_t e = launch_axis_pass_real(n, filt, spec, count, g.tw512, s);
+  if (g_prof) {
+    cudaEventRecord(r.b, s);
+    g_prof_recs.push_back(r);
+  }
+  return e;
+}
+
+// Filter spectra of `count` filters (x, y and, unless xy_only, z passes) into spec. With
+// `real`, filt holds N^3 floats per filter (CONVGPU_FILTER_REAL); spec must not overlap it.
 static cudaError_t enqueue_filter(int n, const float2 *filt, float2 *spec, int count, bool xy_only,
-                                  cudaStream_t s, int tc = 0) {
-  cudaError_t xe = use_xy(n, tc) ? pass_xy(n, filt, spec, count, false, 1.f, s) : cudaErrorNotSupported;
+                                  cudaStream_t s, int tc = 0, bool real = false) {
+  cudaError_t xe = (!real && use_xy(n, tc)) ? pass_xy(n, filt, spec, count, false, 1.f, s) : cudaErrorNotSupported;
   if (xe != cudaSuccess && xe != cudaErrorNotSupported) return xe;
   if (xe == cudaErrorNotSupported) {
-    CG_TRY(pass(n, 0, OP_FWD, filt, spec, nullptr, 0, count, 1.f, s, tc));
+    if (real)
+      CG_TRY(pass_real(n, reinterpret_cast<const float *>(filt), spec, count, s));
+    else
+      CG_TRY(pass(n, 0, OP_FWD, filt, spec, nullptr, 0, count, 1.f, s, tc));
     CG_TRY(pass(n, 1, OP_FWD, spec, spec, nullptr, 0, count, 1.f, s, tc));
   }
   if (!xy_only) CG_TRY(pass(n, 2, OP_FWD, spec, spec, nullptr, 0, count, 1.f, s, tc));
@@ -331,12 +356,13 @@ static cudaError_t enqueue_conv_device(unsigned n, const float2 *sig, const floa
     const long long sv = (flags & kFlagPerSignalFilter) ? V : 0;
     return enqueue_signals(n, sig, out, filt, sv, OP_CONV, how_many, scale, s, nullptr, tc);
   }
+  const bool real = (flags & kFlagFilterReal) != 0;
   if (flags & kFlagPerSignalFilter) {
-    cudaError_t e = enqueue_filter(n, filt, ws, how_many, true, s, tc);
+    cudaError_t e = enqueue_filter(n, filt, ws, how_many, true, s, tc, real);
     if (e != cudaSuccess) return e;
     return enqueue_signals(n, sig, out, ws, V, OP_CONV_FZ, how_many, scale, s, nullptr, tc);
   }
-  cudaError_t e = enqueue_filter(n, filt, ws, 1, false, s, tc);
+  cudaError_t e = enqueue_filter(n, filt, ws, 1, false, s, tc, real);
   if (e != cudaSuccess) return e;
   return enqueue_signals(n, sig, out, ws, 0, OP_CONV, how_many, scale, s, nullptr, tc);
 }
@@ -396,6 +422,14 @@ int bridge_conv_device(unsigned n, const void *d_sig, const void *d_filt, void *
     set_err("invalid arguments");
     return kErrInval;
   }
+  if ((flags & kFlagFilterReal) && (flags & kFlagFilterIsSpectrum)) {
+    set_err("CONVGPU_FILTER_REAL and CONVGPU_FILTER_IS_SPECTRUM exclude each other");
+    return kErrInval;
+  }
+  if ((flags & kFlagFilterReal) && (reinterpret_cast<uintptr_t>(d_filt) & 3u)) {
+    set_err("a real filter must be 4-byte aligned");
+    return kErrInval;
+  }
   if (how_many == 0) return 0;
   std::lock_guard<std::recursive_mutex> lk(g.mu);
   int rc = ensure_init_locked();
@@ -433,6 +467,10 @@ int bridge_conv_uneven_device(const UnevenJob *jobs, unsigned njobs, const void 
       set_err("job with unsupported size");
       return kErrInval;
     }
+  if (flags & kFlagFilterReal) {
+    set_err("CONVGPU_FILTER_REAL is not supported by the uneven-batch entry point");
+    return kErrUnsupported;
+  }
   std::lock_guard<std::recursive_mutex> lk(g.mu);
   int rc = ensure_init_locked();
   if (rc) return rc;
@@ -661,10 +699,12 @@ Timing bridge_conv_host(unsigned n, const void *sig, const void *filt, void *out
   (void)mode;
 
   const bool per_signal = (flags & kFlagPerSignalFilter) != 0;
+  const bool real = (flags & kFlagFilterReal) != 0;  // filt holds N^3 floats per filter
   const size_t V = (size_t)n * n * n;
   const size_t vbytes = V * sizeof(float2);
+  const size_t fbytes = real ? V * sizeof(float) : vbytes;  // bytes of one filter on the host
   const float scale = (flags & kFlagNormalize) ? (float)(1.0 / ((double)V)) : 1.0f;
-  if (!tc && (flags & kFlagHostSlabs) && vbytes >= (size_t(32) << 20)) {
+  if (!tc && !real && (flags & kFlagHostSlabs) && vbytes >= (size_t(32) << 20)) {
     cudaError_t e = conv_host_slabs(n, (const float2 *)sig, (const float2 *)filt, (float2 *)out, how_many, per_signal,
                                     scale, mode, flags, t);
     if (e != cudaSuccess) {
@@ -689,6 +729,10 @@ Timing bridge_conv_host(unsigned n, const void *sig, const void *filt, void *out
     if (e == cudaSuccess && per_signal) e = g.hfio[b].ensure(per_chunk * vbytes);
   }
   if (e == cudaSuccess) e = g.hfilt.ensure(vbytes * (per_signal ? per_chunk : 1));
+  if (real) {  // real filters land in float staging buffers; the x pass widens them
+    for (unsigned b = 0; b < nbuf && e == cudaSuccess && per_signal; ++b) e = g.hreal[b].ensure(per_chunk * fbytes);
+    if (e == cudaSuccess && !per_signal) e = g.hreal[3].ensure(fbytes);
+  }
   if (e != cudaSuccess) {
     cuda_fail(e, "device buffers");
     return t;
@@ -710,15 +754,17 @@ Timing bridge_conv_host(unsigned n, const void *sig, const void *filt, void *out
   for (unsigned b = 0; b < nbuf; ++b) freed[b] = pool.get();
 
   float2 *fspec = (float2 *)g.hfilt.p;
-  const bool cached = filter_cache_hit(filt, n, tc, flags, per_signal);
+  const int key = tc + (real ? 8 : 0);  // path of the kept spectrum
+  const bool cached = filter_cache_hit(filt, n, key, flags, per_signal);
   if (!per_signal && !cached) {
+    float2 *fin = real ? (float2 *)g.hreal[3].p : fspec;
     cudaEventRecord(f0, g.sh2d);
-    e = cudaMemcpyAsync(fspec, filt, vbytes, cudaMemcpyHostToDevice, g.sh2d);
+    e = cudaMemcpyAsync(fin, filt, fbytes, cudaMemcpyHostToDevice, g.sh2d);
     cudaEventRecord(f1, g.sh2d);
     cudaStreamWaitEvent(g.sc, f1, 0);
-    if (e == cudaSuccess) e = enqueue_filter(n, fspec, fspec, 1, false, g.sc, tc);
+    if (e == cudaSuccess) e = enqueue_filter(n, fin, fspec, 1, false, g.sc, tc, real);
     cudaEventRecord(f2, g.sc);
-    if (e == cudaSuccess) filter_cache_set(filt, n, tc, flags, per_signal);
+    if (e == cudaSuccess) filter_cache_set(filt, n, key, flags, per_signal);
   }
 
   // Downloads of chunk c are enqueued after the uploads of chunk c + 1, so a download
@@ -743,16 +789,17 @@ Timing bridge_conv_host(unsigned n, const void *sig, const void *filt, void *out
     if (c >= nbuf) cudaStreamWaitEvent(g.sh2d, freed[b], 0);
     cudaEventRecord(h0[c], g.sh2d);
     e = cudaMemcpyAsync(io, (const float2 *)sig + (size_t)first * V, cnt * vbytes, cudaMemcpyHostToDevice, g.sh2d);
+    void *fin = real ? g.hreal[b].p : g.hfio[b].p;
     if (e == cudaSuccess && per_signal)
-      e = cudaMemcpyAsync(g.hfio[b].p, (const float2 *)filt + (size_t)first * V, cnt * vbytes,
-                          cudaMemcpyHostToDevice, g.sh2d);
+      e = cudaMemcpyAsync(fin, (const char *)filt + (size_t)first * fbytes, cnt * fbytes, cudaMemcpyHostToDevice,
+                          g.sh2d);
     cudaEventRecord(h1[c], g.sh2d);
     if (e != cudaSuccess) break;
     if (c > 0) out_chunk(c - 1);
     cudaStreamWaitEvent(g.sc, h1[c], 0);
     cudaEventRecord(c0[c], g.sc);
     if (per_signal) {
-      e = enqueue_filter(n, (const float2 *)g.hfio[b].p, (float2 *)g.hfio[b].p, cnt, true, g.sc, tc);
+      e = enqueue_filter(n, (const float2 *)fin, (float2 *)g.hfio[b].p, cnt, true, g.sc, tc, real);
       if (e == cudaSuccess)
         e = enqueue_signals(n, io, io, (const float2 *)g.hfio[b].p, (long long)V, OP_CONV_FZ, cnt, scale, g.sc,
                             cm[c], tc);

@@ -19,6 +19,11 @@ cudaError_t launch_axis_pass(int n, int axis, int op, const float2 *src, float2 
                              long long filt_vol_elems, int nvol, float scale, const float2 *tw512,
                              cudaStream_t s);
 
+// x pass of `nvol` cubes of real data (N^3 floats each) into complex dst: the first pass of
+// a real filter's transform (CONVGPU_FILTER_REAL).
+cudaError_t launch_axis_pass_real(int n, const float *src, float2 *dst, int nvol, const float2 *tw512,
+                                  cudaStream_t s);
+
 // Split precision of the tensor-core path.
 constexpr int kTcTf32x3 = 0;
 constexpr int kTcBf16x3 = 1;

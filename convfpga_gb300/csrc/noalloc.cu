@@ -83,10 +83,12 @@ int setup_device(int dev, NoAllocDevice **out) {
 
 int conv_device_noalloc(unsigned n, const void *d_sig, const void *d_filt, void *d_out, unsigned how_many,
                         unsigned flags, void *stream) {
-  constexpr unsigned kNormalize = 1u << 0, kPerSignal = 1u << 1, kIsSpectrum = 1u << 2, kTensor = 1u << 3;
+  constexpr unsigned kNormalize = 1u << 0, kPerSignal = 1u << 1, kIsSpectrum = 1u << 2, kTensor = 1u << 3,
+                     kReal = 1u << 9;
   if (!d_sig || !d_filt || !d_out || n < 16 || n > 512 || (n & (n - 1)) != 0)
     return fail("invalid arguments: null pointer or N not a power of two in 16..512", -1);
   if (flags & kTensor) return fail("the no-allocation entry point runs the plain FP32 path only", -5);
+  if (flags & kReal) return fail("CONVGPU_FILTER_REAL is not supported by the no-allocation entry point", -5);
   if (how_many == 0) return 0;
   const size_t V = (size_t)n * n * n;
   const size_t need = (flags & kIsSpectrum) ? 0 : ((flags & kPerSignal) ? V * how_many : V);

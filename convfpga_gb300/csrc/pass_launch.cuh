@@ -42,6 +42,7 @@ struct PassReq {
   int nvol;     // cubes (z pass); the x / y passes use nplanes
   int nplanes;  // x / y passes: planes of N*N points to transform (a cube is N planes)
   int variant;  // shape variant 0 / 1
+  bool real_src;  // x pass of real rows (a.src holds floats): k_rows_real
   PassArgs a;
   cudaStream_t s;
 };
@@ -182,8 +183,25 @@ static cudaError_t launch_gather_op(const PassReq &r) {
   }
 }
 
+// x pass of real rows (shape variant V's radix plan and rows per CTA).
+template <int N, int V>
+static cudaError_t launch_rows_real(const PassReq &r) {
+  using S = Shape<N, V>;
+  constexpr int E = S::E, XC = S::XC;
+  constexpr int smem = pass_smem_bytes<N, E, XC, true>();
+  auto kern = k_rows_real<N, E, XC, typename S::Plan>;
+  static bool done = false;
+  cudaError_t e = set_smem_once(kern, smem, done);
+  if (e != cudaSuccess) return e;
+  const long long blocks = (long long)r.nplanes * N / XC;
+  if (blocks <= 0 || blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+  kern<<<(unsigned)blocks, XC * (N / E), smem, r.s>>>(r.a);
+  return cudaGetLastError();
+}
+
 template <int N>
 cudaError_t launch_size(const PassReq &r) {
+  if (r.real_src) return r.variant ? launch_rows_real<N, 1>(r) : launch_rows_real<N, 0>(r);
   if (r.mode == kModeGather) return launch_gather_op<N>(r);
   if (r.mode == kModeTable) return launch_tma_variant<N, 0>(r);  // tables are encoded with variant 0
   const cudaError_t e = r.variant ? launch_tma_variant<N, 1>(r) : launch_tma_variant<N, 0>(r);

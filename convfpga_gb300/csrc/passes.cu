@@ -260,6 +260,23 @@ cudaError_t launch_axis_pass_table(int n, int axis, int op, const CUtensorMap *m
   return dispatch(n, r);
 }
 
+cudaError_t launch_axis_pass_real(int n, const float *src, float2 *dst, int nvol, const float2 *tw512,
+                                  cudaStream_t s) {
+  if (nvol <= 0) return cudaSuccess;
+  if (size_index(n) < 0) return cudaErrorInvalidValue;
+  PassReq r{};
+  r.mode = kModeGather;
+  r.axis = 0;
+  r.op = OP_FWD;
+  r.nvol = nvol;
+  r.nplanes = nvol * n;
+  r.variant = get_pass_variant(n, kKindRows);
+  r.real_src = true;
+  r.a = make_args(n, reinterpret_cast<const float2 *>(src), dst, nullptr, 0, 1.f, tw512);
+  r.s = s;
+  return dispatch(n, r);
+}
+
 cudaError_t launch_axis_pass_tc(int n, int axis, int op, const float2 *src, float2 *dst, const float2 *filt,
                                 long long filt_vol_elems, int nvol, float scale, const float2 *tw512,
                                 cudaStream_t s, int prec) {

@@ -179,6 +179,29 @@ __global__ void __launch_bounds__(COLS *(N / E)) k_axis_pass(PassArgs a) {
   for (int e = 0; e < E; ++e) a.dst[base + (long long)(t + e * T) * es] = v[e];
 }
 
+// x pass of real rows (real filters): a.src holds N floats per row; each value enters the
+// transform as (x, 0). Same radix plan and exchange layout as k_rows_tma, so the result
+// equals the complex x pass of the same data with zero imaginary parts, bit for bit.
+template <int N, int E, int XC, class Plan>
+__global__ void __launch_bounds__(XC *(N / E)) k_rows_real(PassArgs a) {
+  constexpr int T = N / E;
+  extern __shared__ float2 smem[];
+  float2 *tw = smem;
+  float2 *sm = smem + N;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = a.tw512[i * (512 / N)];
+  const int t = threadIdx.x % T, c = threadIdx.x / T;
+  const long long row = (long long)blockIdx.x * XC + c;
+  const float *src = reinterpret_cast<const float *>(a.src) + row * N;
+  float2 v[E];
+#pragma unroll
+  for (int e = 0; e < E; ++e) v[e] = make_float2(src[t + e * T], 0.f);
+  __syncthreads();  // twiddle table ready
+  fft_forward<N, E>(v, t, tw, sm, RowSlot<N>{c * row_pitch<N>()}, Plan{});
+  float2 *dst = a.dst + row * N + t;
+#pragma unroll
+  for (int e = 0; e < E; ++e) dst[e * T] = v[e];
+}
+
 // Dynamic shared memory of the TMA-fed x pass: barrier slot, the unpadded row tile (TMA
 // target), the padded exchange buffer, then N twiddles.
 template <int N, int XC>

@@ -30,6 +30,7 @@ extern "C" {
 #define CONVGPU_HOST_SLABS (1u << 7)           /* host batch: stream cubes >= 32 MiB in z-slabs */
 #define CONVGPU_FILTER_CACHED (1u << 8)        /* host batch: shared filter unchanged since the
                                                   last call with this flag, same pointer and N */
+#define CONVGPU_FILTER_REAL (1u << 9)          /* filter is real: N^3 floats per filter cube */
 
 /* Status codes */
 #define CONVGPU_OK 0
@@ -47,6 +48,11 @@ extern "C" {
  * matmuls on the tensor cores with split operands and FP32 accumulation (TF32x3:
  * ~1e-7 relative error per 256-point transform; BF16x3: ~4e-6, which exceeds 1e-5
  * relative L2 end to end on 256^3 convolutions). Other N run the FP32 kernels.
+ * Real filters (CONVGPU_FILTER_REAL): d_filter holds N^3 floats per filter cube (4-byte
+ * aligned); the filter's first pass reads them directly, half the bytes of a complex
+ * filter, and the result equals that of the same filter given as complex values with
+ * zero imaginary parts. Not with CONVGPU_FILTER_IS_SPECTRUM. The reference takes complex
+ * filters only; its real Gaussian filters are stored with zero imaginary parts.
  * d_sig may equal d_out (in place). The library's per-device workspace is shared by
  * all calls: calls on different streams must not overlap. */
 int convgpu_conv3d_device(unsigned N, const float2 *d_sig, const float2 *d_filter, float2 *d_out,
@@ -77,7 +83,8 @@ int convgpu_conv3d_device_noalloc(unsigned N, const float2 *d_sig, const float2 
  * then reuses the spectrum it kept on the device and neither copies nor transforms the
  * filter again (fpga_t reports 0 for both filter fields). Any call that does not hit the
  * cache, and fpga_final, drop the kept spectrum. The reference copies and transforms the
- * filter on every call (host/src/convfpga.c:74-172).
+ * filter on every call (host/src/convfpga.c:74-172). With CONVGPU_FILTER_REAL the host
+ * filter holds N^3 floats per cube and only those bytes are uploaded.
  * Extends fpgaf_conv3D_svm_batch (host/include/convfpga/convfpga.h:46). */
 fpga_t convgpu_conv3d_host(unsigned N, const float2 *sig, const float2 *filter, float2 *out,
                            unsigned how_many, unsigned flags);

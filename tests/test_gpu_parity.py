@@ -346,3 +346,58 @@ def test_host_slab_pipeline_512(gpu):
     t = gpu.conv3d_host(n, sig, filt, out, 1, gpu.HOST_SLABS)
     assert t.valid, gpu.last_error()
     assert snr_db(conv3d(sig, filt, "fp32", engine="pocketfft"), out) > SNR_DB
+
+
+def _real(rng, shape):
+    return rng.uniform(-1, 1, shape).astype(np.float32)
+
+
+@pytest.mark.parametrize("n,per_signal", [(32, False), (64, True), (128, False), (256, True)])
+def test_real_filters_device(gpu, n, per_signal):
+    """CONVGPU_FILTER_REAL on device buffers: the same result, bit for bit, as the complex
+    filter with zero imaginary parts (the real x pass uses the same radix plan and exchange
+    order), and within the reference's SNR criterion of the FP32 oracle."""
+    rng = np.random.default_rng(n + per_signal)
+    b = 2
+    sig = _c64(rng, (b, n, n, n))
+    filt = _real(rng, (b, n, n, n) if per_signal else (n, n, n))
+    flags = gpu.FILTER_PER_SIGNAL if per_signal else 0
+    s = torch.from_numpy(sig).cuda()
+    fr = torch.from_numpy(filt).cuda()
+    fc = torch.from_numpy(filt.astype(np.complex64)).cuda()
+    o_real = torch.empty_like(s)
+    o_cplx = torch.empty_like(s)
+    gpu.conv3d_device(n, s, fr, o_real, b, flags | gpu.FILTER_REAL)
+    gpu.conv3d_device(n, s, fc, o_cplx, b, flags)
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(o_real.cpu().numpy(), o_cplx.cpu().numpy())
+    if n <= 64:
+        ref = conv3d(sig, filt.astype(np.complex64), "fp32", engine="pocketfft")
+        assert snr_db(ref, o_real.cpu().numpy()) > SNR_DB
+    assert gpu.device_status() == 0
+
+
+@pytest.mark.parametrize("per_signal", [False, True])
+def test_real_filters_host(gpu, per_signal):
+    """CONVGPU_FILTER_REAL through the host entry point (float filters on the host, half
+    the filter upload): equal to the complex-filter call."""
+    rng = np.random.default_rng(40 + per_signal)
+    n, b = 64, 5
+    sig = _c64(rng, (b, n, n, n))
+    filt = _real(rng, (b, n, n, n) if per_signal else (n, n, n))
+    flags = gpu.FILTER_PER_SIGNAL if per_signal else 0
+    out_r = np.zeros_like(sig)
+    out_c = np.zeros_like(sig)
+    assert gpu.conv3d_host(n, sig, filt, out_r, b, flags | gpu.FILTER_REAL).valid, gpu.last_error()
+    assert gpu.conv3d_host(n, sig, filt.astype(np.complex64), out_c, b, flags).valid, gpu.last_error()
+    np.testing.assert_array_equal(out_r, out_c)
+
+
+def test_real_filters_rejected_where_unsupported(gpu):
+    n = 32
+    s = torch.zeros((1, n, n, n), dtype=torch.complex64, device="cuda")
+    f = torch.zeros((n, n, n), dtype=torch.float32, device="cuda")
+    with pytest.raises(gpu.ConvGpuError):
+        gpu.conv3d_device(n, s, f, s, 1, gpu.FILTER_REAL | gpu.FILTER_IS_SPECTRUM)
+    with pytest.raises(gpu.ConvGpuError):
+        gpu.conv3d_uneven_device([(n, 0, 0, 0)], s, f, s, gpu.FILTER_REAL)
