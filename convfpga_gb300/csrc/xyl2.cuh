@@ -15,7 +15,13 @@
 //           counter, release add / acquire poll, then fence.proxy.async so the TMA read
 //           sees the generic stores);
 //   X(p, *) with p >= R stores only after all 32 Y(p - R, *) items have read the slot.
-// A CTA holds its current item and the index of its next one; every item it waits on
+// Signals: an X item's "stored" signal is a release add posted by thread 32 as soon as a
+// barrier has ordered every thread's stores before it (planes complete as early as
+// possible: Y items wait on them); a Y item's "slot read" signal is a relaxed add
+// right after its load landed (the data already sits in shared memory, so no later write
+// to the slot can reach it). Thread 0 takes item indices one ahead from the counter, so
+// an atomic's latency is hidden by a whole item.
+// A CTA holds its current item and the indices of the next two; every item it waits on
 // comes earlier in the order (R > L) and its signal is posted as soon as that item ends.
 // So the oldest unfinished item is always some CTA's current item and its dependencies
 // are done: no deadlock, whatever the number of resident CTAs. Every wait is bounded;
@@ -50,6 +56,9 @@ __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
 }
 __device__ __forceinline__ void red_release_add_u32(unsigned *p, unsigned v) {
   asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ void red_relaxed_add_u32(unsigned *p, unsigned v) {
+  asm volatile("red.relaxed.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
 // Polls *p until it reaches `target` (bounded, with back-off). Thread 0 only.
@@ -109,10 +118,12 @@ __global__ void __launch_bounds__(kXyL2Threads, 8) k_xy_l2(const __grid_constant
   const int lag = (int)(np < lag_planes ? np : lag_planes);
   const long long nitems = np * 2LL * kXyL2Items;
 
+  long long ahead = 0;  // thread 0: index of the item after the published one
   if (threadIdx.x == 0) {
     mbar_init(bar, 1);
     mbar_fence_init();
     *next = (long long)atomicAdd(work, 1ull);
+    ahead = (long long)atomicAdd(work, 1ull);
   }
   for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = tw512[2 * i];
   __syncthreads();
@@ -141,8 +152,9 @@ __global__ void __launch_bounds__(kXyL2Threads, 8) k_xy_l2(const __grid_constant
     phase ^= 1u;
     if (threadIdx.x == 0) {
       if (!landed) ok = false;
-      if (is_y) red_release_add_u32(yread + p, 1u);  // slot read: it may be rewritten
-      *next = (long long)atomicAdd(work, 1ull);       // next item, fetched while this one runs
+      if (is_y) red_relaxed_add_u32(yread + p, 1u);  // slot read: it may be rewritten
+      *next = ahead;                                  // published at the end of this item
+      ahead = (long long)atomicAdd(work, 1ull);       // used one item later
     }
     float2 v[E];
     if (is_y) {
