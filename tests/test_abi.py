@@ -83,3 +83,23 @@ def test_workspace_bytes(built_lib):
 def test_fpga_t_layout():
     assert ctypes.sizeof(cg.FpgaTiming) == 56
     assert ctypes.sizeof(cg.Job) == 32
+
+
+def test_flag_and_code_constants_match_the_header():
+    """Every CONVGPU_* flag and return code in include/convgpu.h has the same value in the
+    Python mirror (the mirror is how the tests and the bench pass them)."""
+    import re
+
+    text = open(os.path.join(ROOT, "include", "convgpu.h")).read()
+    defs = dict(re.findall(r"#define CONVGPU_(\w+)\s+\(?(1u << \d+|-?\d+)\)?", text))
+    checked = 0
+    for name, val in defs.items():
+        if not hasattr(cg, name):
+            continue
+        v = 1 << int(val.split("<<")[1]) if "<<" in val else int(val)
+        assert getattr(cg, name) == v, name
+        checked += 1
+    for flag in ("NORMALIZE", "FILTER_PER_SIGNAL", "FILTER_IS_SPECTRUM", "TENSOR_SPLIT", "TENSOR_BF16X3",
+                 "UNEVEN_PER_JOB", "UNEVEN_QUEUE", "HOST_SLABS", "FILTER_CACHED", "FILTER_REAL"):
+        assert flag in defs and hasattr(cg, flag), flag
+    assert checked >= 10
