@@ -51,8 +51,9 @@ def _args():
     p.add_argument("--plan-cache", default=None,
                    help="plan-cache file: loaded instead of autotuning when it exists, written by the "
                         "autotuner otherwise (profiling runs replay the plan of the plain run)")
-    p.add_argument("--workload", choices=["c256x4", "uneven96"], default="c256x4",
-                   help="c256x4: the headline 256^3 x4 workload; uneven96: 96 convolutions of sizes "
+    p.add_argument("--workload", choices=["c256x4", "uneven96", "configs"], default="c256x4",
+                   help="configs: the 64^3 x1, 128^3 x8 and 512^3 x1 workloads on device buffers; "
+                        "c256x4: the headline 256^3 x4 workload; uneven96: 96 convolutions of sizes "
                         "32..256 (work-queue launch vs one job at a time)")
     a = p.parse_args()
     a.warmup = max(a.warmup, 3)
@@ -455,6 +456,73 @@ def run_uneven(a) -> None:
     print(json.dumps(line), flush=True)
 
 
+def run_configs(a) -> None:
+    """The other single-GPU workloads, timed on device buffers (K steps after W warm-up
+    steps, CUDA events): 64^3 x1 (signal and filter U[-1,1], normalised), 128^3 x8 (shared
+    real periodic Gaussian filter, sigma 4) and 512^3 x1 (shared real periodic Gaussian
+    filter, sigma 6). The real filters are passed as floats (CONVGPU_FILTER_REAL). Inputs
+    are generated on the device with the workloads' shapes; for timing, the 512^3 signal is
+    U[-1,1] noise instead of the workload's sum of Gaussian blobs."""
+    import torch
+
+    import convfpga_gb300 as cg
+
+    torch.cuda.set_device(0)
+    if not os.path.exists(cg.LIB_PATH):
+        from convfpga_gb300 import build
+
+        build.build()
+    rc = cg.fpga_initialize("cuda:0", "convgpu_plans.json", False)
+    if rc != 0:
+        raise SystemExit(f"fpga_initialize failed: {rc} {cg.last_error()}")
+    g = torch.Generator(device="cuda").manual_seed(99)
+
+    def uni(shape):
+        return torch.complex(torch.rand(shape, device="cuda", generator=g) * 2 - 1,
+                             torch.rand(shape, device="cuda", generator=g) * 2 - 1)
+
+    def gauss(n, sigma):
+        i = torch.arange(n, device="cuda", dtype=torch.float32)
+        d = torch.minimum(i, n - i) ** 2
+        r2 = d[:, None, None] + d[None, :, None] + d[None, None, :]
+        return torch.exp(-r2 / (2.0 * sigma * sigma)).contiguous()
+
+    results = {}
+    for name, n, b in (("c64x1", 64, 1), ("c128x8", 128, 8), ("c512x1", 512, 1)):
+        cg.autotune([n], write_cache=False)
+        sig = uni((b, n, n, n))
+        if name == "c64x1":
+            filt, flags = uni((n, n, n)), cg.NORMALIZE
+        else:
+            filt, flags = gauss(n, 4.0 if n == 128 else 6.0), cg.FILTER_REAL | cg.NORMALIZE
+        out = torch.empty_like(sig)
+        steps = max(3, a.steps if n < 512 else min(a.steps, 20))
+        for _ in range(a.warmup):
+            cg.conv3d_device(n, sig, filt, out, b, flags)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps):
+            cg.conv3d_device(n, sig, filt, out, b, flags)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        model = (48 + 88 * b) * n ** 3  # one shared filter + b signals, per-axis pass model
+        results[name] = {"conv_per_s": round(b / (ms / 1e3), 1), "ms_per_step": round(ms, 4),
+                         "model_gbs": round(model / (ms / 1e3) / 1e9, 1), "steps": steps,
+                         "filter": "complex U[-1,1]" if name == "c64x1" else "real Gaussian (FILTER_REAL)"}
+        del sig, filt, out
+        torch.cuda.empty_cache()
+    status = cg.device_status()
+    line = {"metric": "3D FFT-conv/s per workload (64^3 x1, 128^3 x8, 512^3 x1), device buffers",
+            "value": results["c128x8"]["conv_per_s"], "unit": "conv/s", "n_gpus": 1, "steps": a.steps,
+            "warmup": a.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded torch generator)", "config": {"workload": "configs", "value_of": "c128x8"},
+            "configs": results, "device_status": status}
+    print(json.dumps(line), flush=True)
+
+
 def _read_traffic(kernel: str):
     """DRAM bytes per launch of the dominant kernel from the committed ncu summary, if any."""
     try:
@@ -469,6 +537,9 @@ def main():
     a = _args()
     if a.workload == "uneven96" and a.impl == "ours":
         run_uneven(a)
+        return
+    if a.workload == "configs" and a.impl == "ours":
+        run_configs(a)
         return
     if a.impl == "reference":
         run_reference(a)
