@@ -31,7 +31,7 @@ template <> struct Shape<128, 1> { static constexpr int E = 16, XC = 8, SC = 16;
 template <> struct Shape<256, 0> { static constexpr int E = 16, XC = 8, SC = 16; using Plan = Radices<16, 16>; };
 template <> struct Shape<256, 1> { static constexpr int E = 16, XC = 16, SC = 8; using Plan = Radices<16, 16>; };
 template <> struct Shape<512, 0> { static constexpr int E = 16, XC = 4, SC = 16; using Plan = Radices<16, 16, 2>; };
-template <> struct Shape<512, 1> { static constexpr int E = 8, XC = 2, SC = 16; using Plan = Radices<8, 8, 8>; };
+template <> struct Shape<512, 1> { static constexpr int E = 16, XC = 8, SC = 8; using Plan = Radices<16, 16, 2>; };
 
 // One pass launch request.
 struct PassReq {
