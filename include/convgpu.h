@@ -162,8 +162,15 @@ int convgpu_autotune(const unsigned *sizes, unsigned count, int write_cache);
 int convgpu_plan_variant(unsigned N, int kind, int set_to);
 
 /* Waits for the device, then returns and clears the library's device status word in
- * *status: 0 when every kernel completed normally; bit 0 set when a kernel gave up a
- * bounded wait for its tile load (it then wrote no output for that tile). */
+ * *status: 0 when every kernel completed normally, otherwise the OR of
+ *   1   a kernel gave up a bounded wait for its tile load (no output for that tile);
+ *   2   the uneven work-queue launch gave up a bounded wait on a dependency;
+ *   4   a tensor-core kernel gave up a bounded wait for its MMA completion;
+ *   8   a tensor-core kernel found its shared memory misaligned and did nothing;
+ *   16  the L2-staged x+y pass gave up a bounded wait on a plane dependency.
+ * Any set bit means the affected outputs are wrong. Host-buffer calls, which wait for
+ * their own kernels, read and clear the word themselves and then return an fpga_t with
+ * valid == 0; stream-ordered device calls leave it for this function. */
 int convgpu_device_status(unsigned *status);
 
 /* Text of the calling thread's last error ("" if none). */
