@@ -22,8 +22,30 @@
 
 namespace convgpu {
 
-__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
-__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+// Complex add / subtract as one packed two-lane FP32 instruction (add/sub.rn.f32x2,
+// sm_100 and later): each lane rounds like a scalar add, half the instructions.
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) {
+  float2 d;
+  asm("{\n\t.reg .b64 pa, pb, pd;\n\t"
+      "mov.b64 pa, {%2, %3};\n\t"
+      "mov.b64 pb, {%4, %5};\n\t"
+      "add.rn.f32x2 pd, pa, pb;\n\t"
+      "mov.b64 {%0, %1}, pd;\n\t}"
+      : "=f"(d.x), "=f"(d.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return d;
+}
+__device__ __forceinline__ float2 csub(float2 a, float2 b) {
+  float2 d;
+  asm("{\n\t.reg .b64 pa, pb, pd;\n\t"
+      "mov.b64 pa, {%2, %3};\n\t"
+      "mov.b64 pb, {%4, %5};\n\t"
+      "sub.rn.f32x2 pd, pa, pb;\n\t"
+      "mov.b64 {%0, %1}, pd;\n\t}"
+      : "=f"(d.x), "=f"(d.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return d;
+}
 // a * b; expression order of comp_mult (kernels/fft/fft_8.cl:180-185).
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
   return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
@@ -126,17 +148,33 @@ struct PlanCheck<N, E, Radices<Rs...>> {
   static constexpr int stages = sizeof...(Rs);
 };
 
+// Twiddle W_N^(r*k*N/(NS*R)) of input r of a butterfly with k = b mod NS, from a linear
+// table tw[j] = W_N^j.
+template <int N, int NS, int R>
+__device__ __forceinline__ float2 stage_tw(const float2 *tw, int r, int k) {
+  return tw[r * k * (N / (NS * R))];
+}
+// The same twiddles for the second stage of a 16 x 16 plan (N = 256) from a table laid out
+// t[r*16 + k] = W_256^(r*k): threads with consecutive k read consecutive entries, where the
+// linear table's r*k strides put up to 8 of a warp's reads in one bank.
+struct TwRT256 {
+  const float2 *t;
+};
+template <int N, int NS, int R>
+__device__ __forceinline__ float2 stage_tw(const TwRT256 &tw, int r, int k) {
+  static_assert(N == 256 && NS == 16 && R == 16, "TwRT256 serves the second stage of a 16 x 16 plan");
+  return tw.t[r * 16 + k];
+}
+
 // One Stockham stage on registers v (t + e*T order on entry). When LAST is false the
 // outputs are written to `sm` via `sidx` and read back in t + e*T order by the caller
-// after a barrier. Twiddles come from `tw` (tw[j] = exp(-2*pi*i*j/N), j < N).
+// after a barrier. Twiddles come from `tw` through stage_tw.
 //
 //   SIdx: functor mapping a pencil position (0..N-1) to a shared-memory slot.
-template <int N, int E, int R, int NS, bool LAST, class SIdx>
-__device__ __forceinline__ void stockham_stage(float2 (&v)[E], int t, const float2 *__restrict__ tw,
-                                               float2 *sm, const SIdx &sidx) {
+template <int N, int E, int R, int NS, bool LAST, class SIdx, class TW>
+__device__ __forceinline__ void stockham_stage(float2 (&v)[E], int t, const TW &tw, float2 *sm, const SIdx &sidx) {
   constexpr int T = N / E;
   constexpr int B = E / R;  // butterflies per thread
-  constexpr int TWSTEP = N / (NS * R);
 #pragma unroll
   for (int i = 0; i < B; ++i) {
     const int b = t + i * T;
@@ -146,7 +184,7 @@ __device__ __forceinline__ void stockham_stage(float2 (&v)[E], int t, const floa
     for (int r = 0; r < R; ++r) x[r] = v[i + r * B];
     if constexpr (NS > 1) {
 #pragma unroll
-      for (int r = 1; r < R; ++r) x[r] = cmul(x[r], tw[r * k * TWSTEP]);
+      for (int r = 1; r < R; ++r) x[r] = cmul(x[r], stage_tw<N, NS, R>(tw, r, k));
     }
     dft<R>(x);
     if constexpr (LAST) {

@@ -73,8 +73,8 @@ struct SwzRow {
   __device__ __forceinline__ int operator()(int n) const { return base + (n ^ ((n >> 4) & 15)); }
 };
 
-template <int N, int E, int NS, class SIdx, int R, int... Rest>
-__device__ __forceinline__ void run_stages(float2 (&v)[E], int t, const float2 *tw, float2 *sm, const SIdx &sidx) {
+template <int N, int E, int NS, class SIdx, class TW, int R, int... Rest>
+__device__ __forceinline__ void run_stages(float2 (&v)[E], int t, const TW &tw, float2 *sm, const SIdx &sidx) {
   constexpr int T = N / E;
   constexpr bool last = sizeof...(Rest) == 0;
   stockham_stage<N, E, R, NS, last>(v, t, tw, sm, sidx);
@@ -83,15 +83,15 @@ __device__ __forceinline__ void run_stages(float2 (&v)[E], int t, const float2 *
 #pragma unroll
     for (int e = 0; e < E; ++e) v[e] = sm[sidx(t + e * T)];
     __syncthreads();
-    run_stages<N, E, NS * R, SIdx, Rest...>(v, t, tw, sm, sidx);
+    run_stages<N, E, NS * R, SIdx, TW, Rest...>(v, t, tw, sm, sidx);
   }
 }
 
-template <int N, int E, class SIdx, int... Rs>
-__device__ __forceinline__ void fft_forward(float2 (&v)[E], int t, const float2 *tw, float2 *sm, const SIdx &sidx,
+template <int N, int E, class SIdx, class TW, int... Rs>
+__device__ __forceinline__ void fft_forward(float2 (&v)[E], int t, const TW &tw, float2 *sm, const SIdx &sidx,
                                             Radices<Rs...>) {
   (void)PlanCheck<N, E, Radices<Rs...>>::stages;
-  run_stages<N, E, 1, SIdx, Rs...>(v, t, tw, sm, sidx);
+  run_stages<N, E, 1, SIdx, TW, Rs...>(v, t, tw, sm, sidx);
 }
 
 template <int E>

@@ -97,6 +97,16 @@ __device__ __forceinline__ void xyl2_item(long long w, long long np, int lag, lo
   }
 }
 
+// Exchange slot of the Y items' in-place transform: ColSlot<8> with the position's lowest
+// bit flipped in odd 16-blocks. A warp holds 4 pencil threads t (t = threadIdx.x / 8); the
+// first stage's stores (positions 16t + r) then fill both halves of the banks instead of
+// putting all four t in the same 16 banks (2 wavefronts per store instead of 4), and the
+// second stage's reads (positions t + 16e) stay two wavefronts.
+struct ColSwz8 {
+  int c;
+  __device__ __forceinline__ int operator()(int n) const { return (n ^ ((n >> 4) & 1)) * 8 + c; }
+};
+
 // msrc: 2D map over the source rows (box {256, 8}); mscr: 3D map over the `ring` scratch
 // planes (box {8, 256, 1}). ctr: 2 * np counters (X stores done, Y reads done) and the
 // work counter at ctr[2 * np], all zero at launch.
@@ -117,7 +127,6 @@ __global__ void __launch_bounds__(kXyL2Threads, 8) k_xy_l2(const __grid_constant
   unsigned long long *work = reinterpret_cast<unsigned long long *>(ctr + 2 * np);
   const int lag = (int)(np < lag_planes ? np : lag_planes);
   const long long nitems = np * 2LL * kXyL2Items;
-
   long long ahead = 0;  // thread 0: index of the item after the published one
   if (threadIdx.x == 0) {
     mbar_init(bar, 1);
@@ -125,7 +134,9 @@ __global__ void __launch_bounds__(kXyL2Threads, 8) k_xy_l2(const __grid_constant
     *next = (long long)atomicAdd(work, 1ull);
     ahead = (long long)atomicAdd(work, 1ull);
   }
-  for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = tw512[2 * i];
+  // t[r*16 + k] = W_256^(r*k) = tw512[2*r*k] (r*k <= 225)
+  for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = tw512[2 * ((i >> 4) * (i & 15))];
+  const TwRT256 twr{tw};
   __syncthreads();
   uint32_t phase = 0;
   bool ok = true;
@@ -159,16 +170,13 @@ __global__ void __launch_bounds__(kXyL2Threads, 8) k_xy_l2(const __grid_constant
     float2 v[E];
     if (is_y) {
       const int c = threadIdx.x % C, t = threadIdx.x / C;
-      const ColSlot<C> sidx{c};
+      const ColSlot<C> lidx{c};  // the TMA box's layout
 #pragma unroll
-      for (int e = 0; e < E; ++e) v[e] = tile[sidx(t + e * T)];
+      for (int e = 0; e < E; ++e) v[e] = tile[lidx(t + e * T)];
       __syncthreads();
       if (INV) swap_all(v);
-      fft_forward<N, E>(v, t, tw, tile, sidx, Plan{});
+      fft_forward<N, E>(v, t, twr, tile, ColSwz8{c}, Plan{});
       if (INV) swap_all(v);
-      float2 *o = dst + p * N * N + tl * C + c;
-#pragma unroll
-      for (int e = 0; e < E; ++e) o[(long long)(t + e * T) * N] = make_float2(v[e].x * scale, v[e].y * scale);
     } else {
       const int t = threadIdx.x % T, c = threadIdx.x / T;
       const SwzRow sidx{c * N};
@@ -176,8 +184,16 @@ __global__ void __launch_bounds__(kXyL2Threads, 8) k_xy_l2(const __grid_constant
       for (int e = 0; e < E; ++e) v[e] = tile[c * N + t + e * T];
       __syncthreads();  // natural-order reads done before the swizzled exchange
       if (INV) swap_all(v);
-      fft_forward<N, E>(v, t, tw, tile, sidx, Plan{});
+      fft_forward<N, E>(v, t, twr, tile, sidx, Plan{});
       if (INV) swap_all(v);
+    }
+    if (is_y) {
+      const int c = threadIdx.x % C, t = threadIdx.x / C;
+      float2 *o = dst + p * N * N + tl * C + c;
+#pragma unroll
+      for (int e = 0; e < E; ++e) o[(long long)(t + e * T) * N] = make_float2(v[e].x * scale, v[e].y * scale);
+    } else {
+      const int t = threadIdx.x % T, c = threadIdx.x / T;
       if (p >= ring) {  // the slot's previous plane must have been read
         if (threadIdx.x == 0 && !wait_count(yread + (p - ring), kXyL2Items)) ok = false;
         __syncthreads();
