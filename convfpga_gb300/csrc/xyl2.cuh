@@ -28,8 +28,10 @@
 // one that gives up sets kStatusQueueWait in the device status word and the CTA carries
 // on (the output is then wrong and the call reports an error).
 //
-// Scratch: R planes of 512 KiB, rewritten every R planes, so its lines stay in the 129 MB
-// L2 between the X store and the Y load and are rarely written back to HBM.
+// Scratch: R = 72 planes of 512 KiB (36 MiB), rewritten every R planes, so its lines stay in
+// the 129 MB L2 between the X store and the Y load and are rarely written back to HBM. The
+// lag (40 planes) and the ring were chosen by timing: a shorter lag or a smaller gap R - L
+// makes items wait on their dependencies, a larger ring no longer stays in L2.
 #pragma once
 
 #include "passes.cuh"
@@ -37,8 +39,8 @@
 namespace convgpu {
 
 constexpr unsigned kStatusQueueWait = 16u;  // a dependency wait of the L2-staged pass gave up
-constexpr int kXyL2Lag = 32;                // L: planes between a plane's X and Y items
-constexpr int kXyL2Ring = 64;               // R: scratch planes (R > L)
+constexpr int kXyL2Lag = 40;                // L: planes between a plane's X and Y items
+constexpr int kXyL2Ring = 72;               // R: scratch planes (R > L)
 constexpr int kXyL2Cols = 8;                // rows per X item, columns per Y item
 constexpr int kXyL2Threads = kXyL2Cols * 16;
 constexpr int kXyL2Items = 256 / kXyL2Cols;  // X (and Y) items per plane
