@@ -19,9 +19,10 @@
 // barrier has ordered every thread's stores before it (planes complete as early as
 // possible: Y items wait on them); a Y item's "slot read" signal is a relaxed add
 // right after its load landed (the data already sits in shared memory, so no later write
-// to the slot can reach it). Thread 0 takes item indices one ahead from the counter, so
-// an atomic's latency is hidden by a whole item.
-// A CTA holds its current item and the indices of the next two; every item it waits on
+// to the slot can reach it). Thread 0 claims the next item's index when the current item's
+// tile has landed and publishes it at the end of the item, so the atomic's latency hides
+// behind the transform.
+// A CTA holds its current item and the index of the next one; every item it waits on
 // comes earlier in the order (R > L) and its signal is posted as soon as that item ends.
 // So the oldest unfinished item is always some CTA's current item and its dependencies
 // are done: no deadlock, whatever the number of resident CTAs. Every wait is bounded;
@@ -129,12 +130,11 @@ __global__ void __launch_bounds__(kXyL2Threads, 8) k_xy_l2(const __grid_constant
   unsigned long long *work = reinterpret_cast<unsigned long long *>(ctr + 2 * np);
   const int lag = (int)(np < lag_planes ? np : lag_planes);
   const long long nitems = np * 2LL * kXyL2Items;
-  long long ahead = 0;  // thread 0: index of the item after the published one
+  long long ahead = 0;  // thread 0: the next item's index, claimed at this item's start
   if (threadIdx.x == 0) {
     mbar_init(bar, 1);
     mbar_fence_init();
     *next = (long long)atomicAdd(work, 1ull);
-    ahead = (long long)atomicAdd(work, 1ull);
   }
   // t[r*16 + k] = W_256^(r*k) = tw512[2*r*k] (r*k <= 225)
   for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = tw512[2 * ((i >> 4) * (i & 15))];
@@ -166,8 +166,7 @@ __global__ void __launch_bounds__(kXyL2Threads, 8) k_xy_l2(const __grid_constant
     if (threadIdx.x == 0) {
       if (!landed) ok = false;
       if (is_y) red_relaxed_add_u32(yread + p, 1u);  // slot read: it may be rewritten
-      *next = ahead;                                  // published at the end of this item
-      ahead = (long long)atomicAdd(work, 1ull);       // used one item later
+      ahead = (long long)atomicAdd(work, 1ull);       // published at the end of this item
     }
     float2 v[E];
     if (is_y) {
@@ -208,6 +207,7 @@ __global__ void __launch_bounds__(kXyL2Threads, 8) k_xy_l2(const __grid_constant
       // thread of another warp than the one issuing the loads signals it.
       if (threadIdx.x == 32) red_release_add_u32(xdone + p, 1u);
     }
+    if (threadIdx.x == 0) *next = ahead;  // the atomic's latency hid behind the transform
     // this item's generic shared-memory writes before the next item's TMA write
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncthreads();  // *next published, tile free
