@@ -343,6 +343,10 @@ static size_t workspace_bytes_for(unsigned n, unsigned how_many, unsigned flags)
   return vol;
 }
 
+// Largest batch for which a shared filter's z transform runs inside the signals' fused z
+// pass instead of as a pass of its own.
+constexpr unsigned kSharedFilterFusedMax = 2;
+
 // Whole convolution on device pointers, enqueued on stream s using workspace ws.
 static cudaError_t enqueue_conv_device(unsigned n, const float2 *sig, const float2 *filt, float2 *out,
                                        unsigned how_many, unsigned flags, float2 *ws, cudaStream_t s) {
@@ -361,6 +365,15 @@ static cudaError_t enqueue_conv_device(unsigned n, const float2 *sig, const floa
     cudaError_t e = enqueue_filter(n, filt, ws, how_many, true, s, tc, real);
     if (e != cudaSuccess) return e;
     return enqueue_signals(n, sig, out, ws, V, OP_CONV_FZ, how_many, scale, s, nullptr, tc);
+  }
+  // A shared filter's z transform is a pass of its own (read + write of one cube) when
+  // its spectrum serves many signals; for one or two signals it is cheaper to redo it
+  // inside each signal's fused z pass (about a quarter of a pass of extra arithmetic per
+  // signal, no extra bytes).
+  if (how_many <= kSharedFilterFusedMax) {
+    cudaError_t e = enqueue_filter(n, filt, ws, 1, true, s, tc, real);
+    if (e != cudaSuccess) return e;
+    return enqueue_signals(n, sig, out, ws, 0, OP_CONV_FZ, how_many, scale, s, nullptr, tc);
   }
   cudaError_t e = enqueue_filter(n, filt, ws, 1, false, s, tc, real);
   if (e != cudaSuccess) return e;

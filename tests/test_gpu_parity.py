@@ -66,6 +66,30 @@ def test_sizes_against_fp32_oracle(gpu, n, per_signal):
     assert rel_l2(ref64, out) < 1e-6
 
 
+@pytest.mark.parametrize("n", [32, 256])
+@pytest.mark.parametrize("how_many", [1, 2, 3])
+def test_shared_filter_batches_against_fp32_oracle(gpu, n, how_many):
+    """A shared filter with one or two signals has its z transform fused into the signals'
+    z pass; from three signals on it gets a pass of its own. Both routes, complex and real
+    filters (the real one bit-identical to the same filter given as complex)."""
+    rng = np.random.default_rng(100 * how_many + n)
+    sig = _c64(rng, (how_many, n, n, n))
+    filt = _c64(rng, (n, n, n))
+    out = dev_conv(gpu, sig, filt)
+    ref = conv3d(sig, filt, "fp32", engine="pocketfft")
+    assert snr_db(ref, out) > SNR_DB
+    g = gaussian_filter(n, 3.0)
+    out_c = dev_conv(gpu, sig, g)
+    s = torch.from_numpy(sig).cuda()
+    fr = torch.from_numpy(np.ascontiguousarray(g.real)).cuda()
+    o = torch.empty_like(s)
+    gpu.conv3d_device(n, s, fr, o, how_many, gpu.FILTER_REAL)
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(o.cpu().numpy(), out_c)
+    assert snr_db(conv3d(sig, g, "fp32", engine="pocketfft"), out_c) > SNR_DB
+    assert gpu.device_status() == 0
+
+
 @pytest.mark.slow
 def test_512_against_fp32_oracle(gpu):
     rng = np.random.default_rng(512)
