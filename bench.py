@@ -401,6 +401,8 @@ def run_uneven(a) -> None:
     if rc != 0:
         raise SystemExit(f"fpga_initialize failed: {rc} {cg.last_error()}")
     sizes = [int(v) for v in np.random.default_rng(4).choice([32, 64, 128, 256], size=96, p=[.4, .3, .2, .1])]
+    # autotuned plan per size (shape variants; fused x+y for the 256^3 jobs), outside the timing
+    cg.autotune(sorted(set(sizes)), write_cache=False)
     offs = np.cumsum([0] + [n ** 3 for n in sizes])
     total = int(offs[-1])
     g = torch.Generator(device="cuda").manual_seed(99)
@@ -453,6 +455,7 @@ def run_uneven(a) -> None:
                        "gpu_launches_per_step": launches_q / a.steps},
         "per_job": {"value": len(sizes) / (ms_j / 1e3), "ms_per_step": ms_j, "gpu_launches_per_step": launches_j / a.steps},
         "speedup_vs_per_job": ms_j / ms_g,
+        "plan": {str(n): {k: cg.plan_variant(n, i) for i, k in enumerate(cg.PLAN_KINDS)} for n in sorted(set(sizes))},
         "gpu_launches": launches_g, "device_status": status, "clocks": clocks,
     }
     print(json.dumps(line), flush=True)

@@ -82,6 +82,15 @@ int uneven_grouped(const struct UnevenJob *jobs, unsigned njobs, const void *d_s
                    void *d_out, bool normalize, const float2 *tw512, cudaStream_t stream, std::string &err);
 void release_grouped_plans();
 void release_xy_l2();
+// L2-staged fused x + y pass (N = 256) over cubes at unrelated addresses (table mode):
+// per-cube rows maps (encode_xy_table_map, in device memory), per-cube output bases and
+// caller-owned dependency counters of xy_l2_counter_bytes(ncubes) bytes. prepare_xy_l2
+// allocates the shared scratch ring and sets the kernel attributes (before a capture).
+cudaError_t prepare_xy_l2();
+size_t xy_l2_counter_bytes(int ncubes);
+bool encode_xy_table_map(CUtensorMap *m, const void *cube);
+cudaError_t launch_xy_l2_table(const CUtensorMap *rmaps, float2 *const *dsts, int ncubes, bool inverse, float scale,
+                               const float2 *tw512, unsigned *status, unsigned *ctr, cudaStream_t s);
 
 // Device address of the status word (for kernels outside passes.cu).
 unsigned int *device_status_address();

@@ -6,7 +6,9 @@
 // brings its own tensor maps and destination base, so the jobs' cubes may sit anywhere.
 // The size classes run as parallel branches of one CUDA graph, captured once per
 // sequence of job sizes and replayed on every call; tensor maps are re-encoded and
-// uploaded only when a job's buffers move.
+// uploaded only when a job's buffers move. When the plan fuses the x and y passes of
+// N = 256 (L2-staged pass), the 256^3 class runs filter x+y, signal x+y, fused z and
+// inverse y+x instead: three table-mode launches of the fused pass around the z launch.
 #include <cuda.h>
 #include <cuda_runtime.h>
 
@@ -24,7 +26,9 @@
 namespace convgpu {
 namespace {
 
-constexpr int kKinds = 7;  // rows(filter) rows(signal) rows(out) y(spec) y(out) z(out) z(spec)
+// rows(filter) rows(signal) rows(out) y(spec) y(out) z(out) z(spec), then the fused x+y
+// pass's rows maps (N = 256): filter, signal, out
+constexpr int kKinds = 10;
 
 struct SizeGroup {
   int n = 0;
@@ -33,6 +37,8 @@ struct SizeGroup {
   float2 **d_dsts = nullptr;      // [0][j] spectrum, [1][j] output
   std::vector<CUtensorMap> h_maps;
   std::vector<float2 *> h_dsts;
+  unsigned *d_ctr = nullptr;  // dependency counters of the fused x+y launches
+  bool xy = false;            // this class runs the fused x+y pass
 };
 
 struct GPlan {
@@ -52,13 +58,15 @@ struct GPlan {
     for (auto &g : groups) {
       if (g.d_maps) cudaFree(g.d_maps);
       if (g.d_dsts) cudaFree(g.d_dsts);
+      if (g.d_ctr) cudaFree(g.d_ctr);
     }
     if (d_spec) cudaFree(d_spec);
   }
 };
 
 std::mutex g_mu;
-std::map<std::pair<std::vector<int>, bool>, std::unique_ptr<GPlan>> g_plans;
+// key: job sizes, normalize + 2 * (fused x+y for N = 256)
+std::map<std::pair<std::vector<int>, int>, std::unique_ptr<GPlan>> g_plans;
 
 cudaError_t enqueue_group(const SizeGroup &g, float scale, const float2 *tw512, cudaStream_t s) {
   const int k = (int)g.jobs.size();
@@ -66,6 +74,14 @@ cudaError_t enqueue_group(const SizeGroup &g, float scale, const float2 *tw512, 
   float2 *const *spec = g.d_dsts;
   float2 *const *out = g.d_dsts + k;
   cudaError_t e;
+  if (g.xy) {
+    unsigned *st = device_status_address();
+    if ((e = launch_xy_l2_table(m + 7 * k, spec, k, false, 1.f, tw512, st, g.d_ctr, s)) != cudaSuccess) return e;
+    if ((e = launch_xy_l2_table(m + 8 * k, out, k, false, 1.f, tw512, st, g.d_ctr, s)) != cudaSuccess) return e;
+    if ((e = launch_axis_pass_table(g.n, 2, OP_CONV_FZ, m + 5 * k, m + 6 * k, out, k, 1.f, tw512, s)) != cudaSuccess)
+      return e;
+    return launch_xy_l2_table(m + 9 * k, out, k, true, scale, tw512, st, g.d_ctr, s);
+  }
   if ((e = launch_axis_pass_table(g.n, 0, OP_FWD, m + 0 * k, nullptr, spec, k, 1.f, tw512, s)) != cudaSuccess) return e;
   if ((e = launch_axis_pass_table(g.n, 0, OP_FWD, m + 1 * k, nullptr, out, k, 1.f, tw512, s)) != cudaSuccess) return e;
   if ((e = launch_axis_pass_table(g.n, 1, OP_FWD, m + 3 * k, nullptr, spec, k, 1.f, tw512, s)) != cudaSuccess) return e;
@@ -76,7 +92,7 @@ cudaError_t enqueue_group(const SizeGroup &g, float scale, const float2 *tw512, 
   return launch_axis_pass_table(g.n, 0, OP_INV, m + 2 * k, nullptr, out, k, scale, tw512, s);
 }
 
-cudaError_t build(GPlan &p, bool normalize, const float2 *tw512) {
+cudaError_t build(GPlan &p, bool normalize, bool xy256, const float2 *tw512) {
   std::map<int, int> idx;
   for (int j = 0; j < (int)p.sizes.size(); ++j) {
     const int n = p.sizes[j];
@@ -103,6 +119,11 @@ cudaError_t build(GPlan &p, bool normalize, const float2 *tw512) {
     g.h_dsts.resize(2 * k);
     if ((e = cudaMalloc(&g.d_maps, sizeof(CUtensorMap) * kKinds * k)) != cudaSuccess) return e;
     if ((e = cudaMalloc(&g.d_dsts, sizeof(float2 *) * 2 * k)) != cudaSuccess) return e;
+    g.xy = xy256 && g.n == 256;
+    if (g.xy) {
+      if ((e = prepare_xy_l2()) != cudaSuccess) return e;
+      if ((e = cudaMalloc(&g.d_ctr, xy_l2_counter_bytes((int)k))) != cudaSuccess) return e;
+    }
   }
   if ((e = cudaEventCreateWithFlags(&p.done, cudaEventDisableTiming)) != cudaSuccess) return e;
   for (auto &g : p.groups)
@@ -158,12 +179,13 @@ int uneven_grouped(const UnevenJob *jobs, unsigned njobs, const void *d_sig, con
       }
   }
   std::lock_guard<std::mutex> lk(g_mu);
-  auto key = std::make_pair(sizes, normalize);
+  const bool xy256 = get_pass_variant(256, kKindXy) == 1;  // the L2-staged variant has a table mode
+  auto key = std::make_pair(sizes, (normalize ? 1 : 0) + (xy256 ? 2 : 0));
   auto it = g_plans.find(key);
   if (it == g_plans.end()) {
     auto p = std::make_unique<GPlan>();
     p->sizes = sizes;
-    cudaError_t e = build(*p, normalize, tw512);
+    cudaError_t e = build(*p, normalize, xy256, tw512);
     if (e != cudaSuccess) {
       err = std::string("uneven grouped plan: ") + cudaGetErrorString(e);
       cudaGetLastError();
@@ -186,6 +208,9 @@ int uneven_grouped(const UnevenJob *jobs, unsigned njobs, const void *d_sig, con
                   encode_table_map(&g.h_maps[2 * k + v], ot, g.n, 0) && encode_table_map(&g.h_maps[3 * k + v], sp, g.n, 1) &&
                   encode_table_map(&g.h_maps[4 * k + v], ot, g.n, 1) && encode_table_map(&g.h_maps[5 * k + v], ot, g.n, 2) &&
                   encode_table_map(&g.h_maps[6 * k + v], sp, g.n, 2);
+        if (ok && g.xy)
+          ok = encode_xy_table_map(&g.h_maps[7 * k + v], ft) && encode_xy_table_map(&g.h_maps[8 * k + v], sg) &&
+               encode_xy_table_map(&g.h_maps[9 * k + v], ot);
         if (!ok) {
           err = "uneven batch: tensor map encoding failed";
           return -5;

@@ -113,12 +113,16 @@ struct ColSwz8 {
 // msrc: 2D map over the source rows (box {256, 8}); mscr: 3D map over the `ring` scratch
 // planes (box {8, 256, 1}). ctr: 2 * np counters (X stores done, Y reads done) and the
 // work counter at ctr[2 * np], all zero at launch.
+// Table mode (rmaps non-null): the planes belong to np / 256 cubes at unrelated
+// addresses; plane p is plane p % 256 of cube p / 256, whose rows map is rmaps[p / 256]
+// (in device memory) and whose output base is dsts[p / 256]; msrc and dst are unused.
 template <bool INV>
 __global__ void __launch_bounds__(kXyL2Threads, 8) k_xy_l2(const __grid_constant__ CUtensorMap msrc,
                                                            const __grid_constant__ CUtensorMap mscr, float2 *scratch,
                                                            float2 *dst, long long np, float scale,
                                                            const float2 *tw512, unsigned *ctr, unsigned *status,
-                                                           int lag_planes, int ring) {
+                                                           int lag_planes, int ring, const CUtensorMap *rmaps,
+                                                           float2 *const *dsts) {
   constexpr int N = 256, E = 16, T = N / E, C = kXyL2Cols;
   using Plan = Radices<16, 16>;
   extern __shared__ __align__(128) unsigned char smraw[];
@@ -156,6 +160,11 @@ __global__ void __launch_bounds__(kXyL2Threads, 8) k_xy_l2(const __grid_constant
         asm volatile("fence.proxy.async.global;" ::: "memory");  // generic stores -> TMA reads
         mbar_arrive_expect_tx(bar, (uint32_t)(C * N * 8));
         tma_load_3d(smem_u32(tile), &mscr, tl * C, 0, slot, bar);
+      } else if (rmaps) {
+        const CUtensorMap *m = rmaps + (p >> 8);
+        tensormap_acquire(m);
+        mbar_arrive_expect_tx(bar, (uint32_t)(C * N * 8));
+        tma_load_2d(smem_u32(tile), m, 0, (int)((p & 255) * N + tl * C), bar);
       } else {
         mbar_arrive_expect_tx(bar, (uint32_t)(C * N * 8));
         tma_load_2d(smem_u32(tile), &msrc, 0, (int)(p * N + tl * C), bar);
@@ -190,7 +199,7 @@ __global__ void __launch_bounds__(kXyL2Threads, 8) k_xy_l2(const __grid_constant
     }
     if (is_y) {
       const int c = threadIdx.x % C, t = threadIdx.x / C;
-      float2 *o = dst + p * N * N + tl * C + c;
+      float2 *o = (rmaps ? dsts[p >> 8] + (p & 255) * N * N : dst + p * N * N) + tl * C + c;
 #pragma unroll
       for (int e = 0; e < E; ++e) o[(long long)(t + e * T) * N] = make_float2(v[e].x * scale, v[e].y * scale);
     } else {

@@ -110,3 +110,34 @@ def test_initialize_ignores_a_file_that_is_not_a_plan_cache(gpu, restore_plans, 
     assert gpu.fpga_initialize("cuda:0", str(p), False) == 0
     gpu.fpga_final()
     assert gpu.fpga_initialize("cuda:0", "convgpu_plans.json", False) == 0
+
+
+def test_uneven_graph_with_fused_xy_256(gpu, restore_plans):
+    """The uneven batch's CUDA graph runs its 256^3 jobs through the table-mode L2-staged
+    x+y pass when the plan fuses x and y (kind 4, variant 1) and through separate passes
+    otherwise; both match the oracle and each other. A second call with new buffers
+    re-encodes the per-job maps of the cached graph."""
+    sizes = [256, 64, 256, 32, 128, 256]
+    offs = np.cumsum([0] + [n ** 3 for n in sizes])
+    outs = {}
+    for xy in (1, 0):
+        gpu.plan_variant(256, 4, xy)
+        for rep in range(2):
+            rng = np.random.default_rng(500 + rep)
+            sigs = [_c64(rng, (n, n, n)) for n in sizes]
+            filts = [_c64(rng, (n, n, n)) for n in sizes]
+            s = torch.from_numpy(np.concatenate([x.ravel() for x in sigs])).cuda()
+            f = torch.from_numpy(np.concatenate([x.ravel() for x in filts])).cuda()
+            o = torch.empty_like(s)
+            jobs = [(n, int(offs[i]), int(offs[i]), int(offs[i])) for i, n in enumerate(sizes)]
+            gpu.conv3d_uneven_device(jobs, s, f, o, gpu.NORMALIZE)
+            torch.cuda.synchronize()
+            oh = o.cpu().numpy()
+            for i, n in enumerate(sizes):
+                ref = conv3d(sigs[i], filts[i], "fp32", normalize=True, engine="pocketfft")
+                assert snr_db(ref, oh[offs[i]:offs[i + 1]].reshape(n, n, n)) > 120.0, (xy, rep, i, n)
+            outs[(xy, rep)] = oh
+            del s, f, o
+    for rep in range(2):
+        assert snr_db(outs[(0, rep)], outs[(1, rep)]) > 130.0
+    assert gpu.device_status() == 0
