@@ -240,7 +240,8 @@ static cudaError_t pass(int n, int axis, int op, const float2 *src, float2 *dst,
   return e;
 }
 
-// Fused x + y pass (N = 256; plan kind kKindXy: 1 L2-staged, 2 8-CTA clusters). Returns
+// Fused x + y pass (plan kind kKindXy: 1 L2-staged (N = 256, 128), 2 8-CTA clusters
+// (N = 256)). Returns
 // cudaErrorNotSupported when it cannot run, in which case the caller runs the x and y
 // passes separately.
 static cudaError_t pass_xy(int n, const float2 *src, float2 *dst, int nvol, bool inverse, float scale,
@@ -267,7 +268,9 @@ static cudaError_t pass_xy(int n, const float2 *src, float2 *dst, int nvol, bool
   return e;
 }
 
-static bool use_xy(int n, int tc) { return tc == 0 && n == 256 && get_pass_variant(n, kKindXy) != 0; }
+static bool use_xy(int n, int tc) {
+  return tc == 0 && (n == 256 || n == 128) && get_pass_variant(n, kKindXy) != 0;
+}
 
 // ------------------------------------------------------------------ pass sequences
 #define CG_TRY(expr)                        \
@@ -943,10 +946,11 @@ int bridge_autotune(const unsigned *sizes, unsigned count, int write_cache) {
     for (int k = 0; k < kPassKinds && err == cudaSuccess; ++k) {
       if (k == kKindXy) {
         // separate x and y passes (variant 0) against the L2-staged fused pass (variant 1);
-        // the cluster pass (variant 2) is not timed: it lost to both on every measurement
+        // the cluster pass (variant 2, N = 256) is not timed: it lost to both on every
+        // measurement
         row.us[0][k] = row.us[row.choice[kKindRows]][kKindRows] + row.us[row.choice[kKindStrided]][kKindStrided];
         row.us[1][k] = 1e30;
-        if (n == 256) {
+        if (n == 256 || n == 128) {
           for (int w = 0; w < 2 && err == cudaSuccess; ++w) {
             err = launch_xy_pass(n, data, data, nvol * n, false, 1.f, g.tw512, s, 1);
             if (err == cudaErrorNotSupported) break;
@@ -960,7 +964,7 @@ int bridge_autotune(const unsigned *sizes, unsigned count, int write_cache) {
             float ms = 0.f;
             cudaEventElapsedTime(&ms, e0, e1);
             row.us[1][k] = 1000.0 * ms / 5.0;
-            count_launches(7);
+            count_launches(14);
           } else if (err == cudaErrorNotSupported) {
             err = cudaSuccess;
           }

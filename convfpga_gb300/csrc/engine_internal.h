@@ -50,10 +50,11 @@ constexpr int kKindRows = 0, kKindStrided = 1, kKindConv = 2, kKindConvFz = 3, k
 int pass_kind(int axis, int op);
 void set_pass_variant(int n, int kind, int variant);
 int get_pass_variant(int n, int kind);
-// Fused x + y pass over `nplanes` planes (N = 256 only; cudaErrorNotSupported otherwise
-// or when tensor maps cannot describe the operands). Plan kind kKindXy: variant 1 stages
-// the x-transformed planes through an L2-resident scratch ring (one persistent kernel),
-// variant 2 keeps each plane in the shared memory of an 8-CTA cluster.
+// Fused x + y pass over `nplanes` planes (N = 256 and 128; cudaErrorNotSupported otherwise
+// or when tensor maps cannot describe the operands). Plan kind kKindXy, N = 256: variant 1
+// stages the x-transformed planes through an L2-resident scratch ring (one persistent
+// kernel), variant 2 keeps each plane in the shared memory of an 8-CTA cluster; N = 128:
+// variant 1 is the L2-staged pass with 16-row / 16-column items.
 cudaError_t launch_xy_pass(int n, const float2 *src, float2 *dst, int nplanes, bool inverse, float scale,
                            const float2 *tw512, cudaStream_t s, int variant);
 // x or y pass (FWD / INV) over `nplanes` consecutive N x N planes starting at src / dst
@@ -82,15 +83,16 @@ int uneven_grouped(const struct UnevenJob *jobs, unsigned njobs, const void *d_s
                    void *d_out, bool normalize, const float2 *tw512, cudaStream_t stream, std::string &err);
 void release_grouped_plans();
 void release_xy_l2();
-// L2-staged fused x + y pass (N = 256) over cubes at unrelated addresses (table mode):
-// per-cube rows maps (encode_xy_table_map, in device memory), per-cube output bases and
-// caller-owned dependency counters of xy_l2_counter_bytes(ncubes) bytes. prepare_xy_l2
-// allocates the shared scratch ring and sets the kernel attributes (before a capture).
-cudaError_t prepare_xy_l2();
-size_t xy_l2_counter_bytes(int ncubes);
-bool encode_xy_table_map(CUtensorMap *m, const void *cube);
-cudaError_t launch_xy_l2_table(const CUtensorMap *rmaps, float2 *const *dsts, int ncubes, bool inverse, float scale,
-                               const float2 *tw512, unsigned *status, unsigned *ctr, cudaStream_t s);
+// L2-staged fused x + y pass (N = 256 or 128) over cubes at unrelated addresses (table
+// mode): per-cube rows maps (encode_xy_table_map, in device memory), per-cube output bases
+// and caller-owned dependency counters of xy_l2_counter_bytes(n, ncubes) bytes.
+// prepare_xy_l2 allocates the size's scratch ring and sets the kernel attributes (call it
+// before a capture).
+cudaError_t prepare_xy_l2(int n);
+size_t xy_l2_counter_bytes(int n, int ncubes);
+bool encode_xy_table_map(CUtensorMap *m, const void *cube, int n);
+cudaError_t launch_xy_l2_table(int n, const CUtensorMap *rmaps, float2 *const *dsts, int ncubes, bool inverse,
+                               float scale, const float2 *tw512, unsigned *status, unsigned *ctr, cudaStream_t s);
 
 // Device address of the status word (for kernels outside passes.cu).
 unsigned int *device_status_address();

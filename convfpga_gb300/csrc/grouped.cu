@@ -7,7 +7,7 @@
 // The size classes run as parallel branches of one CUDA graph, captured once per
 // sequence of job sizes and replayed on every call; tensor maps are re-encoded and
 // uploaded only when a job's buffers move. When the plan fuses the x and y passes of
-// N = 256 (L2-staged pass), the 256^3 class runs filter x+y, signal x+y, fused z and
+// N = 256 or 128 (L2-staged pass), that class runs filter x+y, signal x+y, fused z and
 // inverse y+x instead: three table-mode launches of the fused pass around the z launch.
 #include <cuda.h>
 #include <cuda_runtime.h>
@@ -27,7 +27,7 @@ namespace convgpu {
 namespace {
 
 // rows(filter) rows(signal) rows(out) y(spec) y(out) z(out) z(spec), then the fused x+y
-// pass's rows maps (N = 256): filter, signal, out
+// pass's rows maps (N = 256 and 128): filter, signal, out
 constexpr int kKinds = 10;
 
 struct SizeGroup {
@@ -65,7 +65,7 @@ struct GPlan {
 };
 
 std::mutex g_mu;
-// key: job sizes, normalize + 2 * (fused x+y for N = 256)
+// key: job sizes, normalize + 2 * (fused x+y: bit 0 N = 256, bit 1 N = 128)
 std::map<std::pair<std::vector<int>, int>, std::unique_ptr<GPlan>> g_plans;
 
 cudaError_t enqueue_group(const SizeGroup &g, float scale, const float2 *tw512, cudaStream_t s) {
@@ -76,11 +76,13 @@ cudaError_t enqueue_group(const SizeGroup &g, float scale, const float2 *tw512, 
   cudaError_t e;
   if (g.xy) {
     unsigned *st = device_status_address();
-    if ((e = launch_xy_l2_table(m + 7 * k, spec, k, false, 1.f, tw512, st, g.d_ctr, s)) != cudaSuccess) return e;
-    if ((e = launch_xy_l2_table(m + 8 * k, out, k, false, 1.f, tw512, st, g.d_ctr, s)) != cudaSuccess) return e;
+    if ((e = launch_xy_l2_table(g.n, m + 7 * k, spec, k, false, 1.f, tw512, st, g.d_ctr, s)) != cudaSuccess)
+      return e;
+    if ((e = launch_xy_l2_table(g.n, m + 8 * k, out, k, false, 1.f, tw512, st, g.d_ctr, s)) != cudaSuccess)
+      return e;
     if ((e = launch_axis_pass_table(g.n, 2, OP_CONV_FZ, m + 5 * k, m + 6 * k, out, k, 1.f, tw512, s)) != cudaSuccess)
       return e;
-    return launch_xy_l2_table(m + 9 * k, out, k, true, scale, tw512, st, g.d_ctr, s);
+    return launch_xy_l2_table(g.n, m + 9 * k, out, k, true, scale, tw512, st, g.d_ctr, s);
   }
   if ((e = launch_axis_pass_table(g.n, 0, OP_FWD, m + 0 * k, nullptr, spec, k, 1.f, tw512, s)) != cudaSuccess) return e;
   if ((e = launch_axis_pass_table(g.n, 0, OP_FWD, m + 1 * k, nullptr, out, k, 1.f, tw512, s)) != cudaSuccess) return e;
@@ -92,7 +94,8 @@ cudaError_t enqueue_group(const SizeGroup &g, float scale, const float2 *tw512, 
   return launch_axis_pass_table(g.n, 0, OP_INV, m + 2 * k, nullptr, out, k, scale, tw512, s);
 }
 
-cudaError_t build(GPlan &p, bool normalize, bool xy256, const float2 *tw512) {
+// xy_mask: bit 0 fuses x and y for N = 256, bit 1 for N = 128.
+cudaError_t build(GPlan &p, bool normalize, int xy_mask, const float2 *tw512) {
   std::map<int, int> idx;
   for (int j = 0; j < (int)p.sizes.size(); ++j) {
     const int n = p.sizes[j];
@@ -119,10 +122,10 @@ cudaError_t build(GPlan &p, bool normalize, bool xy256, const float2 *tw512) {
     g.h_dsts.resize(2 * k);
     if ((e = cudaMalloc(&g.d_maps, sizeof(CUtensorMap) * kKinds * k)) != cudaSuccess) return e;
     if ((e = cudaMalloc(&g.d_dsts, sizeof(float2 *) * 2 * k)) != cudaSuccess) return e;
-    g.xy = xy256 && g.n == 256;
+    g.xy = (g.n == 256 && (xy_mask & 1)) || (g.n == 128 && (xy_mask & 2));
     if (g.xy) {
-      if ((e = prepare_xy_l2()) != cudaSuccess) return e;
-      if ((e = cudaMalloc(&g.d_ctr, xy_l2_counter_bytes((int)k))) != cudaSuccess) return e;
+      if ((e = prepare_xy_l2(g.n)) != cudaSuccess) return e;
+      if ((e = cudaMalloc(&g.d_ctr, xy_l2_counter_bytes(g.n, (int)k))) != cudaSuccess) return e;
     }
   }
   if ((e = cudaEventCreateWithFlags(&p.done, cudaEventDisableTiming)) != cudaSuccess) return e;
@@ -179,13 +182,14 @@ int uneven_grouped(const UnevenJob *jobs, unsigned njobs, const void *d_sig, con
       }
   }
   std::lock_guard<std::mutex> lk(g_mu);
-  const bool xy256 = get_pass_variant(256, kKindXy) == 1;  // the L2-staged variant has a table mode
-  auto key = std::make_pair(sizes, (normalize ? 1 : 0) + (xy256 ? 2 : 0));
+  // the L2-staged variant (1) has a table mode
+  const int xy_mask = (get_pass_variant(256, kKindXy) == 1 ? 1 : 0) | (get_pass_variant(128, kKindXy) == 1 ? 2 : 0);
+  auto key = std::make_pair(sizes, (normalize ? 1 : 0) + 2 * xy_mask);
   auto it = g_plans.find(key);
   if (it == g_plans.end()) {
     auto p = std::make_unique<GPlan>();
     p->sizes = sizes;
-    cudaError_t e = build(*p, normalize, xy256, tw512);
+    cudaError_t e = build(*p, normalize, xy_mask, tw512);
     if (e != cudaSuccess) {
       err = std::string("uneven grouped plan: ") + cudaGetErrorString(e);
       cudaGetLastError();
@@ -209,8 +213,8 @@ int uneven_grouped(const UnevenJob *jobs, unsigned njobs, const void *d_sig, con
                   encode_table_map(&g.h_maps[4 * k + v], ot, g.n, 1) && encode_table_map(&g.h_maps[5 * k + v], ot, g.n, 2) &&
                   encode_table_map(&g.h_maps[6 * k + v], sp, g.n, 2);
         if (ok && g.xy)
-          ok = encode_xy_table_map(&g.h_maps[7 * k + v], ft) && encode_xy_table_map(&g.h_maps[8 * k + v], sg) &&
-               encode_xy_table_map(&g.h_maps[9 * k + v], ot);
+          ok = encode_xy_table_map(&g.h_maps[7 * k + v], ft, g.n) &&
+               encode_xy_table_map(&g.h_maps[8 * k + v], sg, g.n) && encode_xy_table_map(&g.h_maps[9 * k + v], ot, g.n);
         if (!ok) {
           err = "uneven batch: tensor map encoding failed";
           return -5;

@@ -243,8 +243,9 @@ namespace convgpu {
 // Tensor-core pass for N = 256 (passes_n256.cu); bf16x3 selects BF16x3 over TF32x3.
 cudaError_t launch_tc256_entry(const PassReq &r, int bf16x3);
 cudaError_t launch_tc05_entry(const PassReq &r);
-cudaError_t launch_xy_l2(const float2 *src, float2 *dst, int nplanes, bool inverse, float scale, const float2 *tw512,
-                         unsigned *status, cudaStream_t s);
+// L2-staged fused x + y pass for N = 256 or 128 (xyl2.cu, xyl2.cuh).
+cudaError_t launch_xy_l2(int n, const float2 *src, float2 *dst, int nplanes, bool inverse, float scale,
+                         const float2 *tw512, unsigned *status, cudaStream_t s);
 // Fused x + y pass for N = 256 on 8-CTA clusters (passes_n256.cu, xy256.cuh).
 cudaError_t launch_xy256(const float2 *src, float2 *dst, int nplanes, bool inverse, float scale, const float2 *tw512,
                          unsigned int *status, cudaStream_t s);

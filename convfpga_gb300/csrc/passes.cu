@@ -305,9 +305,13 @@ cudaError_t launch_axis_pass_tc(int n, int axis, int op, const float2 *src, floa
 
 cudaError_t launch_xy_pass(int n, const float2 *src, float2 *dst, int nplanes, bool inverse, float scale,
                            const float2 *tw512, cudaStream_t s, int variant) {
-  if (n != 256 || !g_use_tma) return cudaErrorNotSupported;
+  if (!g_use_tma) return cudaErrorNotSupported;
+  if (n == 128)
+    return variant == 1 ? launch_xy_l2(128, src, dst, nplanes, inverse, scale, tw512, device_status_address(), s)
+                        : cudaErrorNotSupported;
+  if (n != 256) return cudaErrorNotSupported;
   if (variant == 2) return launch_xy256(src, dst, nplanes, inverse, scale, tw512, device_status_address(), s);
-  return launch_xy_l2(src, dst, nplanes, inverse, scale, tw512, device_status_address(), s);
+  return launch_xy_l2(256, src, dst, nplanes, inverse, scale, tw512, device_status_address(), s);
 }
 
 cudaError_t probe_kernel_image() {

@@ -1,6 +1,6 @@
-// Launcher of the L2-staged fused x + y pass for N = 256 (xyl2.cuh): scratch ring and
-// dependency counters (grow-only, per process), counters cleared on the stream before
-// every launch, one persistent grid of as many CTAs as fit.
+// Launcher of the L2-staged fused x + y pass for N = 256 and 128 (xyl2.cuh): scratch ring
+// per size and dependency counters (grow-only, per process), counters cleared on the
+// stream before every launch, one persistent grid of as many CTAs as fit.
 #define CONVGPU_PASS_LAUNCH_IMPL
 #include "pass_launch.cuh"
 #include "xyl2.cuh"
@@ -35,29 +35,34 @@ struct Scratch {
     bytes = 0;
   }
 };
-Scratch g_ring, g_ctr;
+Scratch g_ring[2], g_ctr;  // scratch rings of N = 256 and N = 128; the process's counters
 }  // namespace
 
 void release_xy_l2() {
-  g_ring.release();
+  g_ring[0].release();
+  g_ring[1].release();
   g_ctr.release();
 }
 
-// The scratch ring (allocated once, never moved) and the kernels' attributes. With
-// max_planes > 0 also the process's own dependency counters (grow-only: reallocated when
-// a launch needs more, so graphs bring their own counters).
-static cudaError_t xy_l2_setup(long long max_planes, int &per_sm, int &sms) {
-  constexpr size_t plane = 256ull * 256 * sizeof(float2);
-  cudaError_t e = g_ring.ensure(plane * kXyL2Ring);
+// The size's scratch ring (allocated once, never moved) and the kernels' attributes.
+// With max_planes > 0 also the process's own dependency counters (grow-only: reallocated
+// when a launch needs more, so graphs bring their own counters).
+template <int N>
+static cudaError_t xy_l2_setup(long long max_planes, int &per_sm, int &sms, Scratch *&ring) {
+  using Cfg = XyL2Cfg<N>;
+  constexpr size_t plane = (size_t)N * N * sizeof(float2);
+  ring = &g_ring[N == 256 ? 0 : 1];
+  cudaError_t e = ring->ensure(plane * Cfg::RING);
   if (e != cudaSuccess) return e;
   const size_t cbytes = (2ull * max_planes + 2) * sizeof(unsigned);
   if (max_planes > 0 && (e = g_ctr.ensure(std::max<size_t>(cbytes, 64 << 10))) != cudaSuccess) return e;
+  constexpr int smem = xyl2_smem<N>();
   static bool done[2] = {false, false};
-  if ((e = set_smem_once(k_xy_l2<false>, kXyL2Smem, done[0])) != cudaSuccess) return e;
-  if ((e = set_smem_once(k_xy_l2<true>, kXyL2Smem, done[1])) != cudaSuccess) return e;
+  if ((e = set_smem_once(k_xy_l2<N, false>, smem, done[0])) != cudaSuccess) return e;
+  if ((e = set_smem_once(k_xy_l2<N, true>, smem, done[1])) != cudaSuccess) return e;
   static int ps = 0, nsm = 0;
   if (ps == 0) {
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ps, (const void *)k_xy_l2<false>, kXyL2Threads, kXyL2Smem) !=
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ps, (const void *)k_xy_l2<N, false>, kXyL2Threads, smem) !=
             cudaSuccess ||
         ps <= 0) {
       cudaGetLastError();
@@ -73,60 +78,74 @@ static cudaError_t xy_l2_setup(long long max_planes, int &per_sm, int &sms) {
   return cudaSuccess;
 }
 
-cudaError_t prepare_xy_l2() {
+cudaError_t prepare_xy_l2(int n) {
   int ps, sms;
-  return xy_l2_setup(0, ps, sms);
+  Scratch *ring;
+  if (n == 256) return xy_l2_setup<256>(0, ps, sms, ring);
+  if (n == 128) return xy_l2_setup<128>(0, ps, sms, ring);
+  return cudaErrorInvalidValue;
 }
 
-size_t xy_l2_counter_bytes(int ncubes) { return (2ull * 256 * ncubes + 2) * sizeof(unsigned); }
+size_t xy_l2_counter_bytes(int n, int ncubes) { return (2ull * n * ncubes + 2) * sizeof(unsigned); }
 
-bool encode_xy_table_map(CUtensorMap *m, const void *cube) {
-  return encode_rows_map(m, cube, 256, 256LL * 256, kXyL2Cols);
+bool encode_xy_table_map(CUtensorMap *m, const void *cube, int n) {
+  if (n == 256) return encode_rows_map(m, cube, 256, 256LL * 256, XyL2Cfg<256>::C);
+  if (n == 128) return encode_rows_map(m, cube, 128, 128LL * 128, XyL2Cfg<128>::C);
+  return false;
 }
 
+template <int N>
 static cudaError_t launch_common(const CUtensorMap *msrc_or_null, const CUtensorMap *rmaps, float2 *const *dsts,
                                  float2 *dst, int nplanes, bool inverse, float scale, const float2 *tw512,
                                  unsigned *status, unsigned *ctr, cudaStream_t s) {
+  using Cfg = XyL2Cfg<N>;
   int ps, sms;
-  cudaError_t e = xy_l2_setup(ctr ? 0 : nplanes, ps, sms);
+  Scratch *ring;
+  cudaError_t e = xy_l2_setup<N>(ctr ? 0 : nplanes, ps, sms, ring);
   if (e != cudaSuccess) return e;
   if (!ctr) ctr = reinterpret_cast<unsigned *>(g_ctr.p);
   CUtensorMap mscr;
-  if (!encode_cube_map(&mscr, g_ring.p, 256, kXyL2Ring, 1, kXyL2Cols)) return cudaErrorNotSupported;
+  if (!encode_cube_map(&mscr, ring->p, N, Cfg::RING, 1, Cfg::C)) return cudaErrorNotSupported;
   const CUtensorMap &msrc = msrc_or_null ? *msrc_or_null : mscr;  // unused in table mode
-  auto kern = inverse ? k_xy_l2<true> : k_xy_l2<false>;
+  auto kern = inverse ? k_xy_l2<N, true> : k_xy_l2<N, false>;
   const long long ncount = 2LL * nplanes + 2;
   k_xyl2_clear<<<(unsigned)std::min<long long>((ncount + 255) / 256, 64), 256, 0, s>>>(ctr, ncount);
-  const long long items = 2LL * nplanes * kXyL2Items;
+  const long long items = 2LL * nplanes * (N / Cfg::C);
   const unsigned grid = (unsigned)std::min<long long>(items, (long long)ps * sms);
-  kern<<<grid, kXyL2Threads, kXyL2Smem, s>>>(msrc, mscr, reinterpret_cast<float2 *>(g_ring.p), dst, nplanes, scale,
-                                             tw512, ctr, status, kXyL2Lag, kXyL2Ring, rmaps, dsts);
+  kern<<<grid, kXyL2Threads, xyl2_smem<N>(), s>>>(msrc, mscr, reinterpret_cast<float2 *>(ring->p), dst, nplanes,
+                                                   scale, tw512, ctr, status, Cfg::LAG, Cfg::RING, rmaps, dsts);
   return cudaGetLastError();
 }
 
-// x then y transform of `nplanes` consecutive 256 x 256 planes, src -> dst (may be the
-// same), inverse transforms with `inverse`, dst scaled by `scale`. The scratch ring and
-// counters are shared by all calls: calls that overlap on the GPU (different streams)
-// must not both run this pass. Returns cudaErrorNotSupported when the operands cannot be
-// described by tensor maps.
-cudaError_t launch_xy_l2(const float2 *src, float2 *dst, int nplanes, bool inverse, float scale, const float2 *tw512,
-                         unsigned *status, cudaStream_t s) {
+// x then y transform of `nplanes` consecutive N x N planes (N = 256 or 128), src -> dst
+// (may be the same), inverse transforms with `inverse`, dst scaled by `scale`. The
+// scratch ring and counters are shared by all calls: calls that overlap on the GPU
+// (different streams) must not both run this pass. Returns cudaErrorNotSupported when the
+// operands cannot be described by tensor maps.
+cudaError_t launch_xy_l2(int n, const float2 *src, float2 *dst, int nplanes, bool inverse, float scale,
+                         const float2 *tw512, unsigned *status, cudaStream_t s) {
   if (nplanes <= 0) return cudaSuccess;
-  if ((reinterpret_cast<uintptr_t>(dst) & 15u) != 0) return cudaErrorNotSupported;
+  if ((reinterpret_cast<uintptr_t>(dst) & 15u) != 0 || (n != 256 && n != 128)) return cudaErrorNotSupported;
   CUtensorMap msrc;
-  if (!encode_rows_map(&msrc, src, 256, (long long)nplanes * 256, kXyL2Cols)) return cudaErrorNotSupported;
-  return launch_common(&msrc, nullptr, nullptr, dst, nplanes, inverse, scale, tw512, status, nullptr, s);
+  const int c = n == 256 ? XyL2Cfg<256>::C : XyL2Cfg<128>::C;
+  if (!encode_rows_map(&msrc, src, n, (long long)nplanes * n, c)) return cudaErrorNotSupported;
+  return n == 256
+             ? launch_common<256>(&msrc, nullptr, nullptr, dst, nplanes, inverse, scale, tw512, status, nullptr, s)
+             : launch_common<128>(&msrc, nullptr, nullptr, dst, nplanes, inverse, scale, tw512, status, nullptr, s);
 }
 
-// The same over `ncubes` 256^3 cubes at unrelated addresses: rmaps[i] (device memory,
-// from encode_xy_table_map) describes the rows of source cube i, dsts[i] is its output
-// base. ctr: the caller's counters, xy_l2_counter_bytes(ncubes) bytes of device memory.
-// Call prepare_xy_l2() first when the launch is captured in a graph.
-cudaError_t launch_xy_l2_table(const CUtensorMap *rmaps, float2 *const *dsts, int ncubes, bool inverse, float scale,
-                               const float2 *tw512, unsigned *status, unsigned *ctr, cudaStream_t s) {
+// The same over `ncubes` N^3 cubes at unrelated addresses: rmaps[i] (device memory, from
+// encode_xy_table_map) describes the rows of source cube i, dsts[i] is its output base.
+// ctr: the caller's counters, xy_l2_counter_bytes(n, ncubes) bytes of device memory. Call
+// prepare_xy_l2(n) first when the launch is captured in a graph.
+cudaError_t launch_xy_l2_table(int n, const CUtensorMap *rmaps, float2 *const *dsts, int ncubes, bool inverse,
+                               float scale, const float2 *tw512, unsigned *status, unsigned *ctr, cudaStream_t s) {
   if (ncubes <= 0) return cudaSuccess;
-  if (!ctr) return cudaErrorInvalidValue;
-  return launch_common(nullptr, rmaps, dsts, nullptr, 256 * ncubes, inverse, scale, tw512, status, ctr, s);
+  if (!ctr || (n != 256 && n != 128)) return cudaErrorInvalidValue;
+  return n == 256 ? launch_common<256>(nullptr, rmaps, dsts, nullptr, 256 * ncubes, inverse, scale, tw512, status,
+                                       ctr, s)
+                  : launch_common<128>(nullptr, rmaps, dsts, nullptr, 128 * ncubes, inverse, scale, tw512, status,
+                                       ctr, s);
 }
 
 }  // namespace convgpu

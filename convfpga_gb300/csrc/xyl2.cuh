@@ -1,5 +1,7 @@
-// Fused x + y pass for N = 256 staged through L2: the x-transformed plane goes to a small
-// ring of scratch planes instead of back to HBM, and the y transform reads it from there.
+// Fused x + y pass for N = 256 and N = 128 staged through L2: the x-transformed plane goes
+// to a small ring of scratch planes instead of back to HBM, and the y transform reads it
+// from there. (Written for N = 256 below; N = 128 uses 16-row / 16-column items, see
+// XyL2Cfg.)
 // A plane then crosses HBM once (read + write) instead of twice, as in the reference's
 // on-chip plane transpose (kernels/conv3D.cl:118-232, transpose + fft3db).
 //
@@ -40,17 +42,8 @@
 namespace convgpu {
 
 constexpr unsigned kStatusQueueWait = 16u;  // a dependency wait of the L2-staged pass gave up
-constexpr int kXyL2Lag = 40;                // L: planes between a plane's X and Y items
-constexpr int kXyL2Ring = 72;               // R: scratch planes (R > L)
-constexpr int kXyL2Cols = 8;                // rows per X item, columns per Y item
-constexpr int kXyL2Threads = kXyL2Cols * 16;
-constexpr int kXyL2Items = 256 / kXyL2Cols;  // X (and Y) items per plane
+constexpr int kXyL2Threads = 128;
 constexpr uint32_t kXyL2Spin = 1u << 20;
-
-// Dynamic shared memory: barrier (128 B), tile (TMA target and exchange buffer), 256
-// twiddles, the next item index: about 18.5 KB, so registers (64 per thread) bound the
-// CTAs per SM at 8.
-constexpr int kXyL2Smem = 128 + kXyL2Cols * 256 * 8 + 256 * 8 + 16;
 
 __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
   unsigned v;
@@ -75,27 +68,28 @@ __device__ __forceinline__ bool wait_count(const unsigned *p, unsigned target) {
   return false;
 }
 
-// Item w of the schedule for `np` planes with lag `lag`: plane, tile, and whether it is a
-// Y item.
+// Item w of the schedule for `np` planes with lag `lag` and `items` X (and Y) items per
+// plane: plane, tile, and whether it is a Y item.
+template <int ITEMS>
 __device__ __forceinline__ void xyl2_item(long long w, long long np, int lag, long long &plane, int &tile,
                                           bool &is_y) {
-  const long long head = (long long)lag * kXyL2Items;     // X only
-  const long long body = (np - lag) * 2LL * kXyL2Items;  // X(b) then Y(b - lag)
+  const long long head = (long long)lag * ITEMS;     // X only
+  const long long body = (np - lag) * 2LL * ITEMS;  // X(b) then Y(b - lag)
   if (w < head) {
-    plane = w / kXyL2Items;
-    tile = (int)(w % kXyL2Items);
+    plane = w / ITEMS;
+    tile = (int)(w % ITEMS);
     is_y = false;
   } else if (w < head + body) {
     const long long v = w - head;
-    const long long b = lag + v / (2 * kXyL2Items);
-    const int r = (int)(v % (2 * kXyL2Items));
-    is_y = r >= kXyL2Items;
+    const long long b = lag + v / (2 * ITEMS);
+    const int r = (int)(v % (2 * ITEMS));
+    is_y = r >= ITEMS;
     plane = is_y ? b - lag : b;
-    tile = is_y ? r - kXyL2Items : r;
+    tile = is_y ? r - ITEMS : r;
   } else {
     const long long v = w - head - body;
-    plane = np - lag + v / kXyL2Items;
-    tile = (int)(v % kXyL2Items);
+    plane = np - lag + v / ITEMS;
+    tile = (int)(v % ITEMS);
     is_y = true;
   }
 }
@@ -110,21 +104,85 @@ struct ColSwz8 {
   __device__ __forceinline__ int operator()(int n) const { return (n ^ ((n >> 4) & 1)) * 8 + c; }
 };
 
-// msrc: 2D map over the source rows (box {256, 8}); mscr: 3D map over the `ring` scratch
-// planes (box {8, 256, 1}). ctr: 2 * np counters (X stores done, Y reads done) and the
+// X items' exchange slot for N = 128 (16 rows of 128 per item): position n of row r at
+// r*128 + (n ^ (((n >> 4) & 7) | ((r & 1) << 3))). A warp holds 4 rows x 8 threads; the
+// first stage's stores (positions 16t + j) and the second stage's loads (t + 8i + 16j)
+// then spread over all 32 banks (two wavefronts, the minimum for 256 bytes) instead of
+// one bank pair.
+struct SwzRow128 {
+  int r;
+  __device__ __forceinline__ int operator()(int n) const { return r * 128 + (n ^ (((n >> 4) & 7) | ((r & 1) << 3))); }
+};
+
+// Twiddles of the second stage of a 16 x 8 plan (N = 128, NS = 16, R = 8) from the table
+// t[j*16 + k] = W_128^(j*k): a warp's threads read consecutive entries.
+struct TwRT128 {
+  const float2 *t;
+};
+template <int N, int NS, int R>
+__device__ __forceinline__ float2 stage_tw(const TwRT128 &tw, int r, int k) {
+  static_assert(N == 128 && NS == 16 && R == 8, "TwRT128 serves the second stage of a 16 x 8 plan");
+  return tw.t[r * 16 + k];
+}
+
+// Per-size shape of the L2-staged pass. C: rows per X item = columns per Y item (each
+// item is C*N = 2048 points for 128 threads of 16 points); LAG / RING: planes between a
+// plane's X and Y items, and scratch planes (R > L; both chosen by timing: a shorter lag
+// or gap R - L makes items wait on their dependencies, a larger ring leaves L2).
+template <int N>
+struct XyL2Cfg;
+template <>
+struct XyL2Cfg<256> {
+  static constexpr int C = 8, LAG = 40, RING = 72;
+  using Plan = Radices<16, 16>;
+  using Tw = TwRT256;
+  // t[r*16 + k] = W_256^(r*k) = tw512[2*r*k] (r*k <= 225)
+  static __device__ __forceinline__ float2 tw_entry(const float2 *tw512, int i) {
+    return tw512[2 * ((i >> 4) * (i & 15))];
+  }
+  static __device__ __forceinline__ SwzRow xslot(int c) { return SwzRow{c * 256}; }
+  static __device__ __forceinline__ ColSwz8 yslot(int c) { return ColSwz8{c}; }
+};
+template <>
+struct XyL2Cfg<128> {
+  // 16 items per plane, so the ~2,400 items the CTAs hold span ~150 planes; the ring is
+  // 288 planes of 128 KiB (36 MiB), the same bytes as N = 256's. Lags of 96..192 planes
+  // time the same within noise.
+  static constexpr int C = 16, LAG = 160, RING = 288;
+  using Plan = Radices<16, 8>;
+  using Tw = TwRT128;
+  // t[j*16 + k] = W_128^(j*k) = tw512[4*j*k] (j < 8, k < 16)
+  static __device__ __forceinline__ float2 tw_entry(const float2 *tw512, int i) {
+    return tw512[4 * ((i >> 4) * (i & 15))];
+  }
+  static __device__ __forceinline__ SwzRow128 xslot(int c) { return SwzRow128{c}; }
+  static __device__ __forceinline__ ColSlot<16> yslot(int c) { return ColSlot<16>{c}; }
+};
+// Dynamic shared memory: barrier (128 B), tile (TMA target and exchange buffer), N
+// twiddles, the next item index: about 18.5 KB, so registers (64 per thread) bound the
+// CTAs per SM at 8.
+template <int N>
+constexpr int xyl2_smem() {
+  return 128 + XyL2Cfg<N>::C * N * 8 + N * 8 + 16;
+}
+
+// msrc: 2D map over the source rows (box {N, C}); mscr: 3D map over the `ring` scratch
+// planes (box {C, N, 1}). ctr: 2 * np counters (X stores done, Y reads done) and the
 // work counter at ctr[2 * np], all zero at launch.
-// Table mode (rmaps non-null): the planes belong to np / 256 cubes at unrelated
-// addresses; plane p is plane p % 256 of cube p / 256, whose rows map is rmaps[p / 256]
-// (in device memory) and whose output base is dsts[p / 256]; msrc and dst are unused.
-template <bool INV>
+// Table mode (rmaps non-null): the planes belong to np / N cubes at unrelated addresses;
+// plane p is plane p % N of cube p / N, whose rows map is rmaps[p / N] (in device
+// memory) and whose output base is dsts[p / N]; msrc and dst are unused.
+template <int N, bool INV>
 __global__ void __launch_bounds__(kXyL2Threads, 8) k_xy_l2(const __grid_constant__ CUtensorMap msrc,
                                                            const __grid_constant__ CUtensorMap mscr, float2 *scratch,
                                                            float2 *dst, long long np, float scale,
                                                            const float2 *tw512, unsigned *ctr, unsigned *status,
                                                            int lag_planes, int ring, const CUtensorMap *rmaps,
                                                            float2 *const *dsts) {
-  constexpr int N = 256, E = 16, T = N / E, C = kXyL2Cols;
-  using Plan = Radices<16, 16>;
+  using Cfg = XyL2Cfg<N>;
+  constexpr int E = 16, T = N / E, C = Cfg::C, ITEMS = N / C;
+  static_assert(C * T == kXyL2Threads, "an item is one pencil tile per thread group");
+  using Plan = typename Cfg::Plan;
   extern __shared__ __align__(128) unsigned char smraw[];
   float2 *tile = reinterpret_cast<float2 *>(smraw + 128);
   float2 *tw = tile + C * N;
@@ -133,16 +191,15 @@ __global__ void __launch_bounds__(kXyL2Threads, 8) k_xy_l2(const __grid_constant
   unsigned *xdone = ctr, *yread = ctr + np;
   unsigned long long *work = reinterpret_cast<unsigned long long *>(ctr + 2 * np);
   const int lag = (int)(np < lag_planes ? np : lag_planes);
-  const long long nitems = np * 2LL * kXyL2Items;
+  const long long nitems = np * 2LL * ITEMS;
   long long ahead = 0;  // thread 0: the next item's index, claimed at this item's start
   if (threadIdx.x == 0) {
     mbar_init(bar, 1);
     mbar_fence_init();
     *next = (long long)atomicAdd(work, 1ull);
   }
-  // t[r*16 + k] = W_256^(r*k) = tw512[2*r*k] (r*k <= 225)
-  for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = tw512[2 * ((i >> 4) * (i & 15))];
-  const TwRT256 twr{tw};
+  for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = Cfg::tw_entry(tw512, i);
+  const typename Cfg::Tw twr{tw};
   __syncthreads();
   uint32_t phase = 0;
   bool ok = true;
@@ -152,19 +209,19 @@ __global__ void __launch_bounds__(kXyL2Threads, 8) k_xy_l2(const __grid_constant
     long long p;
     int tl;
     bool is_y;
-    xyl2_item(w, np, lag, p, tl, is_y);
+    xyl2_item<ITEMS>(w, np, lag, p, tl, is_y);
     const int slot = (int)(p % ring);
     if (threadIdx.x == 0) {
       if (is_y) {
-        if (!wait_count(xdone + p, kXyL2Items)) ok = false;
+        if (!wait_count(xdone + p, ITEMS)) ok = false;
         asm volatile("fence.proxy.async.global;" ::: "memory");  // generic stores -> TMA reads
         mbar_arrive_expect_tx(bar, (uint32_t)(C * N * 8));
         tma_load_3d(smem_u32(tile), &mscr, tl * C, 0, slot, bar);
       } else if (rmaps) {
-        const CUtensorMap *m = rmaps + (p >> 8);
+        const CUtensorMap *m = rmaps + p / N;
         tensormap_acquire(m);
         mbar_arrive_expect_tx(bar, (uint32_t)(C * N * 8));
-        tma_load_2d(smem_u32(tile), m, 0, (int)((p & 255) * N + tl * C), bar);
+        tma_load_2d(smem_u32(tile), m, 0, (int)((p % N) * N + tl * C), bar);
       } else {
         mbar_arrive_expect_tx(bar, (uint32_t)(C * N * 8));
         tma_load_2d(smem_u32(tile), &msrc, 0, (int)(p * N + tl * C), bar);
@@ -185,11 +242,11 @@ __global__ void __launch_bounds__(kXyL2Threads, 8) k_xy_l2(const __grid_constant
       for (int e = 0; e < E; ++e) v[e] = tile[lidx(t + e * T)];
       __syncthreads();
       if (INV) swap_all(v);
-      fft_forward<N, E>(v, t, twr, tile, ColSwz8{c}, Plan{});
+      fft_forward<N, E>(v, t, twr, tile, Cfg::yslot(c), Plan{});
       if (INV) swap_all(v);
     } else {
       const int t = threadIdx.x % T, c = threadIdx.x / T;
-      const SwzRow sidx{c * N};
+      const auto sidx = Cfg::xslot(c);
 #pragma unroll
       for (int e = 0; e < E; ++e) v[e] = tile[c * N + t + e * T];
       __syncthreads();  // natural-order reads done before the swizzled exchange
@@ -199,13 +256,13 @@ __global__ void __launch_bounds__(kXyL2Threads, 8) k_xy_l2(const __grid_constant
     }
     if (is_y) {
       const int c = threadIdx.x % C, t = threadIdx.x / C;
-      float2 *o = (rmaps ? dsts[p >> 8] + (p & 255) * N * N : dst + p * N * N) + tl * C + c;
+      float2 *o = (rmaps ? dsts[p / N] + (p % N) * N * N : dst + p * N * N) + tl * C + c;
 #pragma unroll
       for (int e = 0; e < E; ++e) o[(long long)(t + e * T) * N] = make_float2(v[e].x * scale, v[e].y * scale);
     } else {
       const int t = threadIdx.x % T, c = threadIdx.x / T;
       if (p >= ring) {  // the slot's previous plane must have been read
-        if (threadIdx.x == 0 && !wait_count(yread + (p - ring), kXyL2Items)) ok = false;
+        if (threadIdx.x == 0 && !wait_count(yread + (p - ring), ITEMS)) ok = false;
         __syncthreads();
       }
       float2 *o = scratch + (long long)slot * N * N + (long long)(tl * C + c) * N + t;

@@ -85,6 +85,39 @@ def test_fused_xy_pass_256(gpu, restore_plans, variant, xy):
     assert gpu.device_status() == 0
 
 
+@pytest.mark.parametrize("variant", [0, 1])
+def test_fused_xy_pass_128(gpu, restore_plans, variant):
+    """x and y of 128^3 cubes as one pass staged through an L2-resident scratch ring (plan
+    kind 4, variant 1; 16-row / 16-column items): forward and inverse, shared and
+    per-signal filters, in place, and the host path; the same results as the separate
+    passes within rounding (both within the reference's 120 dB criterion)."""
+    for k in range(KINDS):
+        gpu.plan_variant(128, k, variant)
+    gpu.plan_variant(128, 4, 0)
+    rng = np.random.default_rng(128)
+    sig = _c64(rng, (3, 128, 128, 128))
+    filt = _c64(rng, (3, 128, 128, 128))
+    s = torch.from_numpy(sig).cuda()
+    f = torch.from_numpy(filt).cuda()
+    o_sep = torch.empty_like(s)
+    gpu.conv3d_device(128, s, f, o_sep, 3, gpu.FILTER_PER_SIGNAL)
+    assert gpu.plan_variant(128, 4, 1) == 1
+    _check(gpu, 128, 2, per_signal=False)
+    _check(gpu, 128, 3, per_signal=True)
+    o_xy = torch.empty_like(s)
+    gpu.conv3d_device(128, s, f, o_xy, 3, gpu.FILTER_PER_SIGNAL)
+    s2 = s.clone()
+    gpu.conv3d_device(128, s2, f, s2, 3, gpu.FILTER_PER_SIGNAL | gpu.NORMALIZE)
+    torch.cuda.synchronize()
+    assert snr_db(o_sep.cpu().numpy(), o_xy.cpu().numpy()) > 120.0
+    np.testing.assert_allclose(s2.cpu().numpy(), o_xy.cpu().numpy() / 128 ** 3, rtol=0, atol=1e-6)
+    out = np.zeros_like(sig[:2])
+    t = gpu.fpgaf_conv3D_svm_batch(128, sig[:2], filt[0], out, 2)
+    assert t.valid, gpu.last_error()
+    assert snr_db(conv3d(sig[:2], filt[0], "fp32", engine="pocketfft"), out) > 120.0
+    assert gpu.device_status() == 0
+
+
 def test_autotune_plan_cache_round_trip(gpu, restore_plans, tmp_path):
     path = str(tmp_path / "plans.json")
     gpu.fpga_final()
