@@ -57,12 +57,15 @@ static cudaError_t xy_l2_setup(long long max_planes, int &per_sm, int &sms, Scra
   const size_t cbytes = (2ull * max_planes + 2) * sizeof(unsigned);
   if (max_planes > 0 && (e = g_ctr.ensure(std::max<size_t>(cbytes, 64 << 10))) != cudaSuccess) return e;
   constexpr int smem = xyl2_smem<N>();
-  static bool done[2] = {false, false};
-  if ((e = set_smem_once(k_xy_l2<N, false>, smem, done[0])) != cudaSuccess) return e;
-  if ((e = set_smem_once(k_xy_l2<N, true>, smem, done[1])) != cudaSuccess) return e;
+  static bool done[4] = {false, false, false, false};
+  if ((e = set_smem_once(k_xy_l2<N, false, false>, smem, done[0])) != cudaSuccess) return e;
+  if ((e = set_smem_once(k_xy_l2<N, true, false>, smem, done[1])) != cudaSuccess) return e;
+  if ((e = set_smem_once(k_xy_l2<N, false, true>, smem, done[2])) != cudaSuccess) return e;
+  if ((e = set_smem_once(k_xy_l2<N, true, true>, smem, done[3])) != cudaSuccess) return e;
   static int ps = 0, nsm = 0;
   if (ps == 0) {
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ps, (const void *)k_xy_l2<N, false>, kXyL2Threads, smem) !=
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ps, (const void *)k_xy_l2<N, false, false>, kXyL2Threads,
+                                                      smem) !=
             cudaSuccess ||
         ps <= 0) {
       cudaGetLastError();
@@ -107,7 +110,8 @@ static cudaError_t launch_common(const CUtensorMap *msrc_or_null, const CUtensor
   CUtensorMap mscr;
   if (!encode_cube_map(&mscr, ring->p, N, Cfg::RING, 1, Cfg::C)) return cudaErrorNotSupported;
   const CUtensorMap &msrc = msrc_or_null ? *msrc_or_null : mscr;  // unused in table mode
-  auto kern = inverse ? k_xy_l2<N, true> : k_xy_l2<N, false>;
+  auto kern = rmaps ? (inverse ? k_xy_l2<N, true, true> : k_xy_l2<N, false, true>)
+                    : (inverse ? k_xy_l2<N, true, false> : k_xy_l2<N, false, false>);
   const long long ncount = 2LL * nplanes + 2;
   k_xyl2_clear<<<(unsigned)std::min<long long>((ncount + 255) / 256, 64), 256, 0, s>>>(ctr, ncount);
   const long long items = 2LL * nplanes * (N / Cfg::C);

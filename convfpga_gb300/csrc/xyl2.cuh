@@ -169,10 +169,10 @@ constexpr int xyl2_smem() {
 // msrc: 2D map over the source rows (box {N, C}); mscr: 3D map over the `ring` scratch
 // planes (box {C, N, 1}). ctr: 2 * np counters (X stores done, Y reads done) and the
 // work counter at ctr[2 * np], all zero at launch.
-// Table mode (rmaps non-null): the planes belong to np / N cubes at unrelated addresses;
-// plane p is plane p % N of cube p / N, whose rows map is rmaps[p / N] (in device
-// memory) and whose output base is dsts[p / N]; msrc and dst are unused.
-template <int N, bool INV>
+// TABLE: the planes belong to np / N cubes at unrelated addresses; plane p is plane p % N
+// of cube p / N, whose rows map is rmaps[p / N] (in device memory) and whose output base
+// is dsts[p / N]; msrc and dst are unused (and rmaps, dsts otherwise).
+template <int N, bool INV, bool TABLE>
 __global__ void __launch_bounds__(kXyL2Threads, 8) k_xy_l2(const __grid_constant__ CUtensorMap msrc,
                                                            const __grid_constant__ CUtensorMap mscr, float2 *scratch,
                                                            float2 *dst, long long np, float scale,
@@ -217,11 +217,12 @@ __global__ void __launch_bounds__(kXyL2Threads, 8) k_xy_l2(const __grid_constant
         asm volatile("fence.proxy.async.global;" ::: "memory");  // generic stores -> TMA reads
         mbar_arrive_expect_tx(bar, (uint32_t)(C * N * 8));
         tma_load_3d(smem_u32(tile), &mscr, tl * C, 0, slot, bar);
-      } else if (rmaps) {
-        const CUtensorMap *m = rmaps + p / N;
+      } else if constexpr (TABLE) {
+        const unsigned long long q = (unsigned long long)p;
+        const CUtensorMap *m = rmaps + q / N;
         tensormap_acquire(m);
         mbar_arrive_expect_tx(bar, (uint32_t)(C * N * 8));
-        tma_load_2d(smem_u32(tile), m, 0, (int)((p % N) * N + tl * C), bar);
+        tma_load_2d(smem_u32(tile), m, 0, (int)((q % N) * N + tl * C), bar);
       } else {
         mbar_arrive_expect_tx(bar, (uint32_t)(C * N * 8));
         tma_load_2d(smem_u32(tile), &msrc, 0, (int)(p * N + tl * C), bar);
@@ -256,7 +257,13 @@ __global__ void __launch_bounds__(kXyL2Threads, 8) k_xy_l2(const __grid_constant
     }
     if (is_y) {
       const int c = threadIdx.x % C, t = threadIdx.x / C;
-      float2 *o = (rmaps ? dsts[p / N] + (p % N) * N * N : dst + p * N * N) + tl * C + c;
+      float2 *o;
+      if constexpr (TABLE) {
+        const unsigned long long q = (unsigned long long)p;
+        o = dsts[q / N] + (long long)(q % N) * N * N + tl * C + c;
+      } else {
+        o = dst + p * N * N + tl * C + c;
+      }
 #pragma unroll
       for (int e = 0; e < E; ++e) o[(long long)(t + e * T) * N] = make_float2(v[e].x * scale, v[e].y * scale);
     } else {
