@@ -73,25 +73,37 @@ struct SwzRow {
   __device__ __forceinline__ int operator()(int n) const { return base + (n ^ ((n >> 4) & 15)); }
 };
 
-template <int N, int E, int NS, class SIdx, class TW, int R, int... Rest>
+// Barrier between the exchange's writes and reads: the whole CTA, or only the warp when
+// every pencil's threads and shared-memory slots belong to one warp (WARP).
+template <bool WARP>
+__device__ __forceinline__ void exchange_sync() {
+  if constexpr (WARP)
+    __syncwarp();
+  else
+    __syncthreads();
+}
+
+template <int N, int E, int NS, bool WARP, class SIdx, class TW, int R, int... Rest>
 __device__ __forceinline__ void run_stages(float2 (&v)[E], int t, const TW &tw, float2 *sm, const SIdx &sidx) {
   constexpr int T = N / E;
   constexpr bool last = sizeof...(Rest) == 0;
   stockham_stage<N, E, R, NS, last>(v, t, tw, sm, sidx);
   if constexpr (!last) {
-    __syncthreads();
+    exchange_sync<WARP>();
 #pragma unroll
     for (int e = 0; e < E; ++e) v[e] = sm[sidx(t + e * T)];
-    __syncthreads();
-    run_stages<N, E, NS * R, SIdx, TW, Rest...>(v, t, tw, sm, sidx);
+    exchange_sync<WARP>();
+    run_stages<N, E, NS * R, WARP, SIdx, TW, Rest...>(v, t, tw, sm, sidx);
   }
 }
 
-template <int N, int E, class SIdx, class TW, int... Rs>
+// WARP: the caller guarantees that each pencil's T threads lie in one warp and that no
+// other warp touches its slots, so the exchange needs only warp barriers.
+template <int N, int E, bool WARP = false, class SIdx, class TW, int... Rs>
 __device__ __forceinline__ void fft_forward(float2 (&v)[E], int t, const TW &tw, float2 *sm, const SIdx &sidx,
                                             Radices<Rs...>) {
   (void)PlanCheck<N, E, Radices<Rs...>>::stages;
-  run_stages<N, E, 1, SIdx, TW, Rs...>(v, t, tw, sm, sidx);
+  run_stages<N, E, 1, WARP, SIdx, TW, Rs...>(v, t, tw, sm, sidx);
 }
 
 template <int E>

@@ -250,9 +250,13 @@ __global__ void __launch_bounds__(kXyL2Threads, 8) k_xy_l2(const __grid_constant
       const auto sidx = Cfg::xslot(c);
 #pragma unroll
       for (int e = 0; e < E; ++e) v[e] = tile[c * N + t + e * T];
-      __syncthreads();  // natural-order reads done before the swizzled exchange
+      // A row's T threads are consecutive lanes of one warp (T divides 32) and its slots
+      // are its own: the in-place exchange needs only warp barriers (timed the same as
+      // CTA barriers).
+      static_assert(32 % T == 0, "a row's threads must share a warp");
+      __syncwarp();  // natural-order reads done before the swizzled exchange
       if (INV) swap_all(v);
-      fft_forward<N, E>(v, t, twr, tile, sidx, Plan{});
+      fft_forward<N, E, true>(v, t, twr, tile, sidx, Plan{});
       if (INV) swap_all(v);
     }
     if (is_y) {
