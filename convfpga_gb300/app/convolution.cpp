@@ -7,6 +7,8 @@
 //   -t/--threads T     CPU threads for -c / verify (1)  -b/--batch B  signals (1)
 //   -y/--noverify      skip the CPU check               -c/--cpu-only CPU path only
 //   -s/--usesvm        SVM entry points                  -e/--emulate  emulation platform name
+//   -a/--autotune      time the plan variants for N and write them to the plan-cache file
+//                      (-p) before running: the analogue of building FFTW wisdom
 //
 // Flow as src/main.cpp:11-106: initialise, allocate with fpgaf_complex_malloc, fill with
 // rand()/RAND_MAX, run the entry point the flags select (fpgaf_conv3D, fpgaf_conv3D_svm,
@@ -37,7 +39,7 @@ struct Config {
   std::string path;
   std::string wisdomfile = "a.out";
   unsigned num = 64, iter = 1, threads = 1, batch = 1;
-  bool noverify = false, cpuonly = false, usesvm = false, emulate = false;
+  bool noverify = false, cpuonly = false, usesvm = false, emulate = false, autotune = false;
 };
 
 void usage() {
@@ -53,6 +55,7 @@ void usage() {
       "  -c, --cpu-only      CPU convolution only\n"
       "  -s, --usesvm        SVM entry points\n"
       "  -e, --emulate       emulation platform name\n"
+      "  -a, --autotune      tune the plan for N and write it to the plan-cache file\n"
       "  -h, --help          this text\n");
 }
 
@@ -79,6 +82,7 @@ bool parse(int argc, char **argv, Config &c) {
     else if (a == "-c" || a == "--cpu-only") c.cpuonly = true;
     else if (a == "-s" || a == "--usesvm") c.usesvm = true;
     else if (a == "-e" || a == "--emulate") c.emulate = true;
+    else if (a == "-a" || a == "--autotune") c.autotune = true;
     else {
       std::fprintf(stderr, "Error parsing options: unknown option %s\n", a.c_str());
       return false;
@@ -254,6 +258,14 @@ int main(int argc, char **argv) {
   if (fpga_initialize(platform, c.path.c_str(), c.usesvm) != 0) {
     std::fprintf(stderr, "FPGA initialization error\n");
     return EXIT_FAILURE;
+  }
+  if (c.autotune) {
+    const unsigned sizes[1] = {c.num};
+    if (convgpu_autotune(sizes, 1, 1) != 0) {
+      std::fprintf(stderr, "autotune error: %s\n", convgpu_last_error());
+      return EXIT_FAILURE;
+    }
+    std::printf("Plan for %u^3 tuned and written to %s\n", c.num, c.path.c_str());
   }
   float2 *filter = (float2 *)fpgaf_complex_malloc(sizeof(float2) * pts);
   float2 *sig = (float2 *)fpgaf_complex_malloc(sizeof(float2) * pts * c.batch);

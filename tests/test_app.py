@@ -53,3 +53,19 @@ def test_gpu_runs_verify(app, args):
     r = _run(app, "-p", "convgpu_plans.json", *args)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "verified" in r.stdout and "Measurements in ms" in r.stdout
+
+
+@pytest.mark.gpu
+def test_gpu_autotune_writes_the_plan_cache(app, tmp_path):
+    """-a tunes the plan for N and writes it to the -p file (the wisdom-file analogue); a
+    second run reads it back."""
+    import json
+
+    path = str(tmp_path / "plans.json")
+    r = _run(app, "-p", path, "-n", "32", "-a")
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "tuned and written" in r.stdout and "verified" in r.stdout
+    plans = json.load(open(path))
+    assert "32" in plans["sizes"]
+    r = _run(app, "-p", path, "-n", "32")
+    assert r.returncode == 0, r.stdout + r.stderr
