@@ -240,7 +240,7 @@ static cudaError_t pass(int n, int axis, int op, const float2 *src, float2 *dst,
   return e;
 }
 
-// Fused x + y pass (plan kind kKindXy: 1 L2-staged (N = 256, 128), 2 8-CTA clusters
+// Fused x + y pass (plan kind kKindXy: 1 L2-staged (N = 128, 256, 512), 2 8-CTA clusters
 // (N = 256)). Returns
 // cudaErrorNotSupported when it cannot run, in which case the caller runs the x and y
 // passes separately.
@@ -269,7 +269,7 @@ static cudaError_t pass_xy(int n, const float2 *src, float2 *dst, int nvol, bool
 }
 
 static bool use_xy(int n, int tc) {
-  return tc == 0 && (n == 256 || n == 128) && get_pass_variant(n, kKindXy) != 0;
+  return tc == 0 && (n == 128 || n == 256 || n == 512) && get_pass_variant(n, kKindXy) != 0;
 }
 
 // ------------------------------------------------------------------ pass sequences
@@ -950,7 +950,7 @@ int bridge_autotune(const unsigned *sizes, unsigned count, int write_cache) {
         // measurement
         row.us[0][k] = row.us[row.choice[kKindRows]][kKindRows] + row.us[row.choice[kKindStrided]][kKindStrided];
         row.us[1][k] = 1e30;
-        if (n == 256 || n == 128) {
+        if (n == 128 || n == 256 || n == 512) {
           for (int w = 0; w < 2 && err == cudaSuccess; ++w) {
             err = launch_xy_pass(n, data, data, nvol * n, false, 1.f, g.tw512, s, 1);
             if (err == cudaErrorNotSupported) break;

@@ -50,11 +50,11 @@ constexpr int kKindRows = 0, kKindStrided = 1, kKindConv = 2, kKindConvFz = 3, k
 int pass_kind(int axis, int op);
 void set_pass_variant(int n, int kind, int variant);
 int get_pass_variant(int n, int kind);
-// Fused x + y pass over `nplanes` planes (N = 256 and 128; cudaErrorNotSupported otherwise
+// Fused x + y pass over `nplanes` planes (N = 128, 256, 512; cudaErrorNotSupported otherwise
 // or when tensor maps cannot describe the operands). Plan kind kKindXy, N = 256: variant 1
 // stages the x-transformed planes through an L2-resident scratch ring (one persistent
-// kernel), variant 2 keeps each plane in the shared memory of an 8-CTA cluster; N = 128:
-// variant 1 is the L2-staged pass with 16-row / 16-column items.
+// kernel), variant 2 keeps each plane in the shared memory of an 8-CTA cluster; N = 128
+// and 512: variant 1 is the L2-staged pass (16-row / 16-column and 4-row / 4-column items).
 cudaError_t launch_xy_pass(int n, const float2 *src, float2 *dst, int nplanes, bool inverse, float scale,
                            const float2 *tw512, cudaStream_t s, int variant);
 // x or y pass (FWD / INV) over `nplanes` consecutive N x N planes starting at src / dst

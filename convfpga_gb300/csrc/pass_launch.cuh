@@ -51,6 +51,7 @@ constexpr int kModeTma = 0, kModeTable = 1, kModeGather = 2;
 // Tensor-map encoders (passes.cu). Return false when the operand cannot be described.
 bool encode_cube_map(CUtensorMap *m, const void *base, int n, long long nplanes, int axis, int cols);
 bool encode_rows_map(CUtensorMap *m, const void *base, int n, long long rows, int xc);
+bool encode_rows512_map(CUtensorMap *m, const void *base, long long rows, int xc);
 
 template <int N>
 cudaError_t launch_size(const PassReq &r);
@@ -243,7 +244,7 @@ namespace convgpu {
 // Tensor-core pass for N = 256 (passes_n256.cu); bf16x3 selects BF16x3 over TF32x3.
 cudaError_t launch_tc256_entry(const PassReq &r, int bf16x3);
 cudaError_t launch_tc05_entry(const PassReq &r);
-// L2-staged fused x + y pass for N = 256 or 128 (xyl2.cu, xyl2.cuh).
+// L2-staged fused x + y pass for N = 128, 256 or 512 (xyl2.cu, xyl2.cuh).
 cudaError_t launch_xy_l2(int n, const float2 *src, float2 *dst, int nplanes, bool inverse, float scale,
                          const float2 *tw512, unsigned *status, cudaStream_t s);
 // Fused x + y pass for N = 256 on 8-CTA clusters (passes_n256.cu, xy256.cuh).

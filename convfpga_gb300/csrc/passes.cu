@@ -81,6 +81,22 @@ bool encode_rows_map(CUtensorMap *m, const void *base, int n, long long rows, in
   return r == CUDA_SUCCESS;
 }
 
+// Tensor map over `rows` rows of 512 complex64 viewed as (x, half, row) = (256, 2, rows),
+// box {256, 2, xc}: one load lands xc whole rows, each contiguous in shared memory (a
+// 2D box is at most 256 wide).
+bool encode_rows512_map(CUtensorMap *m, const void *base, long long rows, int xc) {
+  auto enc = tensor_map_encoder();
+  if (!enc || (reinterpret_cast<uintptr_t>(base) & 15u) != 0 || rows > 0x7fffffffLL) return false;
+  cuuint64_t dims[3] = {256, 2, (cuuint64_t)rows};
+  cuuint64_t strides[2] = {256 * 8, 512 * 8};
+  cuuint32_t box[3] = {256, 2, (cuuint32_t)xc};
+  cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_UINT64, 3, const_cast<void *>(base), dims, strides, box, estr,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
 // Box shapes of shape variant 0 (the variant table-mode launches use).
 static void v0_shape(int n, int &xc, int &sc) {
   switch (n) {
@@ -306,8 +322,8 @@ cudaError_t launch_axis_pass_tc(int n, int axis, int op, const float2 *src, floa
 cudaError_t launch_xy_pass(int n, const float2 *src, float2 *dst, int nplanes, bool inverse, float scale,
                            const float2 *tw512, cudaStream_t s, int variant) {
   if (!g_use_tma) return cudaErrorNotSupported;
-  if (n == 128)
-    return variant == 1 ? launch_xy_l2(128, src, dst, nplanes, inverse, scale, tw512, device_status_address(), s)
+  if (n == 128 || n == 512)
+    return variant == 1 ? launch_xy_l2(n, src, dst, nplanes, inverse, scale, tw512, device_status_address(), s)
                         : cudaErrorNotSupported;
   if (n != 256) return cudaErrorNotSupported;
   if (variant == 2) return launch_xy256(src, dst, nplanes, inverse, scale, tw512, device_status_address(), s);

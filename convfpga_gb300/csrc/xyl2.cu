@@ -1,5 +1,5 @@
-// Launcher of the L2-staged fused x + y pass for N = 256 and 128 (xyl2.cuh): scratch ring
-// per size and dependency counters (grow-only, per process), counters cleared on the
+// Launcher of the L2-staged fused x + y pass for N = 128, 256 and 512 (xyl2.cuh): scratch
+// ring per size and dependency counters (grow-only, per process), counters cleared on the
 // stream before every launch, one persistent grid of as many CTAs as fit.
 #define CONVGPU_PASS_LAUNCH_IMPL
 #include "pass_launch.cuh"
@@ -35,12 +35,11 @@ struct Scratch {
     bytes = 0;
   }
 };
-Scratch g_ring[2], g_ctr;  // scratch rings of N = 256 and N = 128; the process's counters
+Scratch g_ring[3], g_ctr;  // scratch rings of N = 256, 128 and 512; the process's counters
 }  // namespace
 
 void release_xy_l2() {
-  g_ring[0].release();
-  g_ring[1].release();
+  for (auto &r : g_ring) r.release();
   g_ctr.release();
 }
 
@@ -51,7 +50,7 @@ template <int N>
 static cudaError_t xy_l2_setup(long long max_planes, int &per_sm, int &sms, Scratch *&ring) {
   using Cfg = XyL2Cfg<N>;
   constexpr size_t plane = (size_t)N * N * sizeof(float2);
-  ring = &g_ring[N == 256 ? 0 : 1];
+  ring = &g_ring[N == 256 ? 0 : (N == 128 ? 1 : 2)];
   cudaError_t e = ring->ensure(plane * Cfg::RING);
   if (e != cudaSuccess) return e;
   const size_t cbytes = (2ull * max_planes + 2) * sizeof(unsigned);
@@ -86,15 +85,23 @@ cudaError_t prepare_xy_l2(int n) {
   Scratch *ring;
   if (n == 256) return xy_l2_setup<256>(0, ps, sms, ring);
   if (n == 128) return xy_l2_setup<128>(0, ps, sms, ring);
+  if (n == 512) return xy_l2_setup<512>(0, ps, sms, ring);
   return cudaErrorInvalidValue;
 }
 
 size_t xy_l2_counter_bytes(int n, int ncubes) { return (2ull * n * ncubes + 2) * sizeof(unsigned); }
 
-bool encode_xy_table_map(CUtensorMap *m, const void *cube, int n) {
-  if (n == 256) return encode_rows_map(m, cube, 256, 256LL * 256, XyL2Cfg<256>::C);
-  if (n == 128) return encode_rows_map(m, cube, 128, 128LL * 128, XyL2Cfg<128>::C);
+// The source rows map of the pass: 2D rows (box {N, C}) for N <= 256; for N = 512 rows
+// viewed as (256, 2, rows) with box {256, 2, C}, since a box is at most 256 long.
+static bool encode_xy_rows(CUtensorMap *m, const void *src, int n, long long rows) {
+  if (n == 256) return encode_rows_map(m, src, 256, rows, XyL2Cfg<256>::C);
+  if (n == 128) return encode_rows_map(m, src, 128, rows, XyL2Cfg<128>::C);
+  if (n == 512) return encode_rows512_map(m, src, rows, XyL2Cfg<512>::C);
   return false;
+}
+
+bool encode_xy_table_map(CUtensorMap *m, const void *cube, int n) {
+  return encode_xy_rows(m, cube, n, (long long)n * n);
 }
 
 template <int N>
@@ -121,7 +128,7 @@ static cudaError_t launch_common(const CUtensorMap *msrc_or_null, const CUtensor
   return cudaGetLastError();
 }
 
-// x then y transform of `nplanes` consecutive N x N planes (N = 256 or 128), src -> dst
+// x then y transform of `nplanes` consecutive N x N planes (N = 128, 256 or 512), src -> dst
 // (may be the same), inverse transforms with `inverse`, dst scaled by `scale`. The
 // scratch ring and counters are shared by all calls: calls that overlap on the GPU
 // (different streams) must not both run this pass. Returns cudaErrorNotSupported when the
@@ -129,13 +136,15 @@ static cudaError_t launch_common(const CUtensorMap *msrc_or_null, const CUtensor
 cudaError_t launch_xy_l2(int n, const float2 *src, float2 *dst, int nplanes, bool inverse, float scale,
                          const float2 *tw512, unsigned *status, cudaStream_t s) {
   if (nplanes <= 0) return cudaSuccess;
-  if ((reinterpret_cast<uintptr_t>(dst) & 15u) != 0 || (n != 256 && n != 128)) return cudaErrorNotSupported;
+  if ((reinterpret_cast<uintptr_t>(dst) & 15u) != 0) return cudaErrorNotSupported;
   CUtensorMap msrc;
-  const int c = n == 256 ? XyL2Cfg<256>::C : XyL2Cfg<128>::C;
-  if (!encode_rows_map(&msrc, src, n, (long long)nplanes * n, c)) return cudaErrorNotSupported;
-  return n == 256
-             ? launch_common<256>(&msrc, nullptr, nullptr, dst, nplanes, inverse, scale, tw512, status, nullptr, s)
-             : launch_common<128>(&msrc, nullptr, nullptr, dst, nplanes, inverse, scale, tw512, status, nullptr, s);
+  if (!encode_xy_rows(&msrc, src, n, (long long)nplanes * n)) return cudaErrorNotSupported;
+  switch (n) {
+    case 256: return launch_common<256>(&msrc, nullptr, nullptr, dst, nplanes, inverse, scale, tw512, status, nullptr, s);
+    case 128: return launch_common<128>(&msrc, nullptr, nullptr, dst, nplanes, inverse, scale, tw512, status, nullptr, s);
+    case 512: return launch_common<512>(&msrc, nullptr, nullptr, dst, nplanes, inverse, scale, tw512, status, nullptr, s);
+    default: return cudaErrorNotSupported;
+  }
 }
 
 // The same over `ncubes` N^3 cubes at unrelated addresses: rmaps[i] (device memory, from
@@ -145,11 +154,13 @@ cudaError_t launch_xy_l2(int n, const float2 *src, float2 *dst, int nplanes, boo
 cudaError_t launch_xy_l2_table(int n, const CUtensorMap *rmaps, float2 *const *dsts, int ncubes, bool inverse,
                                float scale, const float2 *tw512, unsigned *status, unsigned *ctr, cudaStream_t s) {
   if (ncubes <= 0) return cudaSuccess;
-  if (!ctr || (n != 256 && n != 128)) return cudaErrorInvalidValue;
-  return n == 256 ? launch_common<256>(nullptr, rmaps, dsts, nullptr, 256 * ncubes, inverse, scale, tw512, status,
-                                       ctr, s)
-                  : launch_common<128>(nullptr, rmaps, dsts, nullptr, 128 * ncubes, inverse, scale, tw512, status,
-                                       ctr, s);
+  if (!ctr) return cudaErrorInvalidValue;
+  switch (n) {
+    case 256: return launch_common<256>(nullptr, rmaps, dsts, nullptr, 256 * ncubes, inverse, scale, tw512, status, ctr, s);
+    case 128: return launch_common<128>(nullptr, rmaps, dsts, nullptr, 128 * ncubes, inverse, scale, tw512, status, ctr, s);
+    case 512: return launch_common<512>(nullptr, rmaps, dsts, nullptr, 512 * ncubes, inverse, scale, tw512, status, ctr, s);
+    default: return cudaErrorInvalidValue;
+  }
 }
 
 }  // namespace convgpu

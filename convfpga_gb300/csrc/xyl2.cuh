@@ -1,7 +1,7 @@
-// Fused x + y pass for N = 256 and N = 128 staged through L2: the x-transformed plane goes
-// to a small ring of scratch planes instead of back to HBM, and the y transform reads it
-// from there. (Written for N = 256 below; N = 128 uses 16-row / 16-column items, see
-// XyL2Cfg.)
+// Fused x + y pass for N = 128, 256 and 512 staged through L2: the x-transformed plane
+// goes to a small ring of scratch planes instead of back to HBM, and the y transform reads
+// it from there. (Written for N = 256 below; N = 128 uses 16-row / 16-column items and
+// N = 512 4-row / 4-column items, see XyL2Cfg.)
 // A plane then crosses HBM once (read + write) instead of twice, as in the reference's
 // on-chip plane transpose (kernels/conv3D.cl:118-232, transpose + fft3db).
 //
@@ -125,6 +125,31 @@ __device__ __forceinline__ float2 stage_tw(const TwRT128 &tw, int r, int k) {
   return tw.t[r * 16 + k];
 }
 
+// Y items' exchange slot for N = 512 (4 columns per item): ColSlot<4> with the position's
+// low 2 bits XOR bits 4..5. A warp holds 8 consecutive pencil threads t x 4 columns; the
+// first stage's stores (positions 16t + j), the later stages' loads (t + 32e) and the
+// second stage's stores ((t/16)*256 + t%16 + 16j) then spread over all 32 banks (two
+// wavefronts) instead of 8 lanes per bank pair.
+struct ColSwz4 {
+  int c;
+  __device__ __forceinline__ int operator()(int n) const { return (n ^ ((n >> 4) & 3)) * 4 + c; }
+};
+
+// Twiddles of a 16 x 16 x 2 plan (N = 512): entries 0..255 hold W_512^(2*r*k) at r*16 + k
+// (second stage, NS = 16, R = 16: a warp reads consecutive entries), entries 256..767 hold
+// W_512^j (third stage, NS = 256, R = 2).
+struct TwRT512 {
+  const float2 *t;
+};
+template <int N, int NS, int R>
+__device__ __forceinline__ float2 stage_tw(const TwRT512 &tw, int r, int k) {
+  static_assert(N == 512 && ((NS == 16 && R == 16) || (NS == 256 && R == 2)), "TwRT512 serves a 16 x 16 x 2 plan");
+  if constexpr (NS == 16)
+    return tw.t[r * 16 + k];
+  else
+    return tw.t[256 + r * k];
+}
+
 // Per-size shape of the L2-staged pass. C: rows per X item = columns per Y item (each
 // item is C*N = 2048 points for 128 threads of 16 points); LAG / RING: planes between a
 // plane's X and Y items, and scratch planes (R > L; both chosen by timing: a shorter lag
@@ -133,7 +158,7 @@ template <int N>
 struct XyL2Cfg;
 template <>
 struct XyL2Cfg<256> {
-  static constexpr int C = 8, LAG = 40, RING = 72;
+  static constexpr int C = 8, LAG = 40, RING = 72, TWN = 256;
   using Plan = Radices<16, 16>;
   using Tw = TwRT256;
   // t[r*16 + k] = W_256^(r*k) = tw512[2*r*k] (r*k <= 225)
@@ -142,13 +167,20 @@ struct XyL2Cfg<256> {
   }
   static __device__ __forceinline__ SwzRow xslot(int c) { return SwzRow{c * 256}; }
   static __device__ __forceinline__ ColSwz8 yslot(int c) { return ColSwz8{c}; }
+  // C rows from the rows map / C columns of a scratch plane, one box each
+  static __device__ __forceinline__ void load_x(uint32_t d, const CUtensorMap *m, int row0, uint32_t bar) {
+    tma_load_2d(d, m, 0, row0, bar);
+  }
+  static __device__ __forceinline__ void load_y(uint32_t d, const CUtensorMap *m, int x0, int slot, uint32_t bar) {
+    tma_load_3d(d, m, x0, 0, slot, bar);
+  }
 };
 template <>
 struct XyL2Cfg<128> {
   // 16 items per plane, so the ~2,400 items the CTAs hold span ~150 planes; the ring is
   // 288 planes of 128 KiB (36 MiB), the same bytes as N = 256's. Lags of 96..192 planes
   // time the same within noise.
-  static constexpr int C = 16, LAG = 160, RING = 288;
+  static constexpr int C = 16, LAG = 160, RING = 288, TWN = 128;
   using Plan = Radices<16, 8>;
   using Tw = TwRT128;
   // t[j*16 + k] = W_128^(j*k) = tw512[4*j*k] (j < 8, k < 16)
@@ -157,13 +189,43 @@ struct XyL2Cfg<128> {
   }
   static __device__ __forceinline__ SwzRow128 xslot(int c) { return SwzRow128{c}; }
   static __device__ __forceinline__ ColSlot<16> yslot(int c) { return ColSlot<16>{c}; }
+  static __device__ __forceinline__ void load_x(uint32_t d, const CUtensorMap *m, int row0, uint32_t bar) {
+    tma_load_2d(d, m, 0, row0, bar);
+  }
+  static __device__ __forceinline__ void load_y(uint32_t d, const CUtensorMap *m, int x0, int slot, uint32_t bar) {
+    tma_load_3d(d, m, x0, 0, slot, bar);
+  }
 };
-// Dynamic shared memory: barrier (128 B), tile (TMA target and exchange buffer), N
-// twiddles, the next item index: about 18.5 KB, so registers (64 per thread) bound the
+template <>
+struct XyL2Cfg<512> {
+  // 256 items per plane: the ~2,400 items the CTAs hold span ~10 planes. The ring is 18
+  // planes of 2 MiB (36 MiB, as for the other sizes); lag / ring 8 / 16 and 14 / 24 time
+  // no better.
+  static constexpr int C = 4, LAG = 10, RING = 18, TWN = 768;
+  using Plan = Radices<16, 16, 2>;
+  using Tw = TwRT512;
+  static __device__ __forceinline__ float2 tw_entry(const float2 *tw512, int i) {
+    return i < 256 ? tw512[2 * ((i >> 4) * (i & 15))] : tw512[i - 256];
+  }
+  // a row's 512 slots: the low 4 bits XOR bits 4..7 (one row per warp, 32 threads)
+  static __device__ __forceinline__ SwzRow xslot(int c) { return SwzRow{c * 512}; }
+  static __device__ __forceinline__ ColSwz4 yslot(int c) { return ColSwz4{c}; }
+  // rows map viewed as (256, 2, rows): one box lands C whole rows
+  static __device__ __forceinline__ void load_x(uint32_t d, const CUtensorMap *m, int row0, uint32_t bar) {
+    tma_load_3d(d, m, 0, 0, row0, bar);
+  }
+  // a box is at most 256 long: rows 0..255 and 256..511 of the C columns
+  static __device__ __forceinline__ void load_y(uint32_t d, const CUtensorMap *m, int x0, int slot, uint32_t bar) {
+    tma_load_3d(d, m, x0, 0, slot, bar);
+    tma_load_3d(d + 256 * C * 8, m, x0, 256, slot, bar);
+  }
+};
+// Dynamic shared memory: barrier (128 B), tile (TMA target and exchange buffer), the
+// twiddle table, the next item index: 18-23 KB, so registers (64 per thread) bound the
 // CTAs per SM at 8.
 template <int N>
 constexpr int xyl2_smem() {
-  return 128 + XyL2Cfg<N>::C * N * 8 + N * 8 + 16;
+  return 128 + XyL2Cfg<N>::C * N * 8 + XyL2Cfg<N>::TWN * 8 + 16;
 }
 
 // msrc: 2D map over the source rows (box {N, C}); mscr: 3D map over the `ring` scratch
@@ -186,7 +248,7 @@ __global__ void __launch_bounds__(kXyL2Threads, 8) k_xy_l2(const __grid_constant
   extern __shared__ __align__(128) unsigned char smraw[];
   float2 *tile = reinterpret_cast<float2 *>(smraw + 128);
   float2 *tw = tile + C * N;
-  long long *next = reinterpret_cast<long long *>(tw + N);
+  long long *next = reinterpret_cast<long long *>(tw + Cfg::TWN);
   const uint32_t bar = smem_u32(smraw);
   unsigned *xdone = ctr, *yread = ctr + np;
   unsigned long long *work = reinterpret_cast<unsigned long long *>(ctr + 2 * np);
@@ -198,7 +260,7 @@ __global__ void __launch_bounds__(kXyL2Threads, 8) k_xy_l2(const __grid_constant
     mbar_fence_init();
     *next = (long long)atomicAdd(work, 1ull);
   }
-  for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = Cfg::tw_entry(tw512, i);
+  for (int i = threadIdx.x; i < Cfg::TWN; i += blockDim.x) tw[i] = Cfg::tw_entry(tw512, i);
   const typename Cfg::Tw twr{tw};
   __syncthreads();
   uint32_t phase = 0;
@@ -216,16 +278,16 @@ __global__ void __launch_bounds__(kXyL2Threads, 8) k_xy_l2(const __grid_constant
         if (!wait_count(xdone + p, ITEMS)) ok = false;
         asm volatile("fence.proxy.async.global;" ::: "memory");  // generic stores -> TMA reads
         mbar_arrive_expect_tx(bar, (uint32_t)(C * N * 8));
-        tma_load_3d(smem_u32(tile), &mscr, tl * C, 0, slot, bar);
+        Cfg::load_y(smem_u32(tile), &mscr, tl * C, slot, bar);
       } else if constexpr (TABLE) {
         const unsigned long long q = (unsigned long long)p;
         const CUtensorMap *m = rmaps + q / N;
         tensormap_acquire(m);
         mbar_arrive_expect_tx(bar, (uint32_t)(C * N * 8));
-        tma_load_2d(smem_u32(tile), m, 0, (int)((q % N) * N + tl * C), bar);
+        Cfg::load_x(smem_u32(tile), m, (int)((q % N) * N + tl * C), bar);
       } else {
         mbar_arrive_expect_tx(bar, (uint32_t)(C * N * 8));
-        tma_load_2d(smem_u32(tile), &msrc, 0, (int)(p * N + tl * C), bar);
+        Cfg::load_x(smem_u32(tile), &msrc, (int)(p * N + tl * C), bar);
       }
     }
     const bool landed = __syncthreads_and(mbar_wait_bounded(bar, phase) ? 1 : 0);

@@ -156,7 +156,7 @@ int convgpu_autotune(const unsigned *sizes, unsigned count, int write_cache);
 /* Plan-table entry of cube size N for pass kind (0 x pass, 1 y/z passes, 2 fused z pass,
  * 3 fused z pass with the filter's z transform, 4 x and y: 0 separate passes; N = 256:
  * 1 one pass staged through an L2-resident scratch ring, 2 one pass on 8-CTA clusters;
- * N = 128: 1 one pass staged through an L2-resident scratch ring;
+ * N = 128 and 512: 1 one pass staged through an L2-resident scratch ring;
  * 5 tensor-core kernels of CONVGPU_TENSOR_SPLIT, N = 256: 0 tcgen05 (TMEM accumulators),
  * 1 mma.sync): sets it to set_to (0 or 1; 0..2 for kind 4) when set_to >= 0, and returns
  * the current variant (or a negative CONVGPU_E* code). */

@@ -174,3 +174,36 @@ def test_uneven_graph_with_fused_xy_256(gpu, restore_plans):
     for rep in range(2):
         assert snr_db(outs[(0, rep)], outs[(1, rep)]) > 130.0
     assert gpu.device_status() == 0
+
+
+@pytest.mark.slow
+def test_fused_xy_pass_512(gpu, restore_plans):
+    """x and y of 512^3 cubes as one L2-staged pass (plan kind 4, variant 1; 4-row /
+    4-column items, two TMA boxes per column tile): a shifted delta filter gives the
+    circular shift of the signal, and the result equals the separate passes' within
+    rounding, forward and inverse."""
+    n = 512
+    rng = np.random.default_rng(512)
+    sig = np.empty((1, n, n, n), np.complex64)
+    sig.real = rng.standard_normal((1, n, n, n), dtype=np.float32)
+    sig.imag = rng.standard_normal((1, n, n, n), dtype=np.float32)
+    delta = np.zeros((n, n, n), np.complex64)
+    delta[3, 5, 7] = 1.0
+    s = torch.from_numpy(sig).cuda()
+    d = torch.from_numpy(delta).cuda()
+    f = torch.from_numpy(_c64(rng, (n, n, n))).cuda()
+    outs = {}
+    for xy in (0, 1):
+        assert gpu.plan_variant(n, 4, xy) == xy
+        o = torch.empty_like(s)
+        gpu.conv3d_device(n, s, d, o, 1, gpu.NORMALIZE)
+        torch.cuda.synchronize()
+        shifted = np.roll(sig, shift=(3, 5, 7), axis=(1, 2, 3))
+        from oracle import rel_l2
+        assert rel_l2(shifted, o.cpu().numpy()) < 1e-6, xy
+        gpu.conv3d_device(n, s, f, o, 1, 0)
+        torch.cuda.synchronize()
+        outs[xy] = o.cpu().numpy()
+        del o
+    assert snr_db(outs[0], outs[1]) > 120.0
+    assert gpu.device_status() == 0
