@@ -107,15 +107,21 @@ def test_tc_256_spectrum_reuse(gpu, tc_kernel):
     assert rel_l2(ref, out) <= REL_L2_TC
 
 
-@pytest.mark.parametrize("n", [32, 128])
-def test_tc_flag_on_sizes_without_tc_kernels(gpu, n):
-    """Sizes with no tensor-core kernel run the FP32 kernels: bit-identical results."""
-    rng = np.random.default_rng(n)
-    sig = (rng.uniform(-1, 1, (2, n, n, n)) + 1j * rng.uniform(-1, 1, (2, n, n, n))).astype(np.complex64)
-    filt = (rng.uniform(-1, 1, (n, n, n)) + 1j * rng.uniform(-1, 1, (n, n, n))).astype(np.complex64)
-    a = _run(gpu, sig, filt, gpu.TENSOR_SPLIT)
-    b = _run(gpu, sig, filt, 0)
-    np.testing.assert_array_equal(a, b)
+@pytest.mark.parametrize("n,xy", [(32, 0), (128, 0), (128, 1)])
+def test_tc_flag_on_sizes_without_tc_kernels(gpu, n, xy):
+    """Sizes with no tensor-core kernel run the FP32 kernels, the fused x+y pass included
+    when the plan chooses it: bit-identical results."""
+    keep = gpu.plan_variant(n, 4)
+    gpu.plan_variant(n, 4, xy)
+    try:
+        rng = np.random.default_rng(n)
+        sig = (rng.uniform(-1, 1, (2, n, n, n)) + 1j * rng.uniform(-1, 1, (2, n, n, n))).astype(np.complex64)
+        filt = (rng.uniform(-1, 1, (n, n, n)) + 1j * rng.uniform(-1, 1, (n, n, n))).astype(np.complex64)
+        a = _run(gpu, sig, filt, gpu.TENSOR_SPLIT)
+        b = _run(gpu, sig, filt, 0)
+        np.testing.assert_array_equal(a, b)
+    finally:
+        gpu.plan_variant(n, 4, keep)
 
 
 def test_tc_host_entry_point(gpu):
