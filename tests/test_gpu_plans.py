@@ -145,16 +145,17 @@ def test_initialize_ignores_a_file_that_is_not_a_plan_cache(gpu, restore_plans, 
     assert gpu.fpga_initialize("cuda:0", "convgpu_plans.json", False) == 0
 
 
-def test_uneven_graph_with_fused_xy_256(gpu, restore_plans):
-    """The uneven batch's CUDA graph runs its 256^3 jobs through the table-mode L2-staged
-    x+y pass when the plan fuses x and y (kind 4, variant 1) and through separate passes
-    otherwise; both match the oracle and each other. A second call with new buffers
+def test_uneven_graph_with_fused_xy(gpu, restore_plans):
+    """The uneven batch's CUDA graph runs its 256^3 and 128^3 jobs through the table-mode
+    L2-staged x+y pass when the plan fuses x and y (kind 4, variant 1) and through separate
+    passes otherwise; both match the oracle and each other. A second call with new buffers
     re-encodes the per-job maps of the cached graph."""
-    sizes = [256, 64, 256, 32, 128, 256]
+    sizes = [256, 64, 256, 32, 128, 256, 128]
     offs = np.cumsum([0] + [n ** 3 for n in sizes])
     outs = {}
     for xy in (1, 0):
         gpu.plan_variant(256, 4, xy)
+        gpu.plan_variant(128, 4, xy)
         for rep in range(2):
             rng = np.random.default_rng(500 + rep)
             sigs = [_c64(rng, (n, n, n)) for n in sizes]
