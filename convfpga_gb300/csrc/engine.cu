@@ -366,6 +366,16 @@ static cudaError_t enqueue_conv_device(unsigned n, const float2 *sig, const floa
     return enqueue_signals(n, sig, out, filt, sv, OP_CONV, how_many, scale, s, nullptr, tc);
   }
   const bool real = (flags & kFlagFilterReal) != 0;
+  // One small cube (N <= 64, 2 MiB, L2-resident): the whole convolution in one cooperative
+  // launch instead of seven launches separated by launch gaps.
+  if (how_many == 1 && tc == 0 && !real && n <= 64) {
+    const cudaError_t e = launch_small_conv((int)n, sig, filt, out, ws, scale, g.tw512, device_status_address(), s);
+    if (e == cudaSuccess) {
+      count_launches(1);
+      return cudaSuccess;
+    }
+    cudaGetLastError();  // not applicable (size, residency): the per-pass launches below
+  }
   if (flags & kFlagPerSignalFilter) {
     cudaError_t e = enqueue_filter(n, filt, ws, how_many, true, s, tc, real);
     if (e != cudaSuccess) return e;

@@ -286,6 +286,56 @@ __global__ void __launch_bounds__(kPThreads, 3) k_persistent_queue(const UJob *_
   }
 }
 
+// ------------------------------------------------------------------ small cubes, one launch
+// One convolution of a small cube (N <= 64) as a single cooperative launch: the seven
+// passes in their five dependency levels ({filter x, signal x}, {filter y, signal y},
+// fused z, y inverse, x inverse), each level's tiles spread over the grid, a grid barrier
+// between levels. A 64^3 cube is 2 MiB and stays in L2, so separate launches are bound by
+// launch gaps, not by HBM. The cooperative launch makes every block resident, so the
+// barrier cannot wait on a block that never runs; each wait is still bounded and one that
+// gives up sets kStatusQueueTimeout.
+// Barrier k (k = 1..4) of a launch waits until its counter reaches k * gridDim.x; every
+// launch uses its own counter slot, zeroed before use.
+__device__ __forceinline__ bool small_grid_barrier(unsigned *slot, unsigned target, unsigned *status) {
+  __shared__ int s_ok;
+  __syncthreads();  // this block's stores for the level are done
+  if (threadIdx.x == 0) {
+    __threadfence();  // ... and visible device-wide before the arrival
+    atomicAdd(slot, 1u);
+    int ok = 1;
+    uint32_t spins = 0;
+    while ((unsigned)ld_acquire(reinterpret_cast<const int *>(slot)) < target) {
+      if (++spins > kSpinLimit) {
+        ok = 0;
+        if (status) atomicOr(status, kStatusQueueTimeout);
+        break;
+      }
+      __nanosleep(32);
+    }
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+// Pass i of dependency level lv (levels 0 and 1 have two passes, the others one).
+__device__ __forceinline__ int small_level_pass(int lv, int i) { return lv < 2 ? 2 * lv + i : lv + 2; }
+
+template <int N>
+__global__ void __launch_bounds__(kPThreads, 3) k_small_conv(UJob j, unsigned *slot, const float2 *tw512,
+                                                             unsigned *status) {
+  extern __shared__ __align__(128) unsigned char smraw[];
+  const int nt = ptiles(N);
+  for (int lv = 0; lv < 5; ++lv) {
+    const int npass = lv < 2 ? 2 : 1;
+    for (int w = blockIdx.x; w < npass * nt; w += gridDim.x) {
+      run_tile<N>(j, small_level_pass(lv, w / nt), w % nt, smraw, tw512);
+      __syncthreads();  // shared buffers are reused by the next tile
+    }
+    if (lv < 4 && !small_grid_barrier(slot, (unsigned)(lv + 1) * gridDim.x, status)) return;
+  }
+}
+
 // ------------------------------------------------------------------ host side
 namespace {
 
@@ -313,6 +363,8 @@ struct PPlan {
 
 std::mutex g_pmu;
 std::map<std::vector<int>, std::unique_ptr<PPlan>> g_plans;
+unsigned *g_small_slots = nullptr;  // barrier counters of the small-cube launches (a ring)
+unsigned long long g_small_next = 0;
 std::string g_perr;
 
 cudaError_t build_plan(PPlan &p, const float2 *tw512, unsigned *status) {
@@ -424,6 +476,53 @@ int uneven_persistent(const UnevenJob *jobs, unsigned njobs, const void *d_sig, 
 void release_uneven_plans() {
   std::lock_guard<std::mutex> lk(g_pmu);
   g_plans.clear();
+  if (g_small_slots) cudaFree(g_small_slots);
+  g_small_slots = nullptr;
+  g_small_next = 0;
+}
+
+// One convolution of an N^3 cube (N = 16, 32 or 64) in one cooperative launch: sig and
+// filt are N^3 complex64 each, spec is N^3 of workspace for the filter spectrum.
+// cudaErrorNotSupported for other N or when the grid cannot be co-resident.
+cudaError_t launch_small_conv(int n, const float2 *sig, const float2 *filt, float2 *out, float2 *spec, float scale,
+                              const float2 *tw512, unsigned *status, cudaStream_t s) {
+  constexpr int kSlots = 1024;
+  if (n != 16 && n != 32 && n != 64) return cudaErrorNotSupported;
+  std::lock_guard<std::mutex> lk(g_pmu);
+  cudaError_t e;
+  if (!g_small_slots) {
+    if ((e = cudaMalloc(&g_small_slots, kSlots * sizeof(unsigned))) != cudaSuccess) return e;
+    g_small_next = 0;
+  }
+  if (g_small_next % kSlots == 0) {  // a fresh (or wrapped) ring: every slot back to zero
+    if ((e = cudaMemsetAsync(g_small_slots, 0, kSlots * sizeof(unsigned), s)) != cudaSuccess) return e;
+  }
+  unsigned *slot = g_small_slots + (g_small_next++ % kSlots);
+  void (*kern)(UJob, unsigned *, const float2 *, unsigned *) =
+      n == 16 ? k_small_conv<16> : (n == 32 ? k_small_conv<32> : k_small_conv<64>);
+  static bool attr[3] = {false, false, false};
+  const int ai = n == 16 ? 0 : (n == 32 ? 1 : 2);
+  if (!attr[ai]) {
+    if ((e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kPSmemBytes)) != cudaSuccess)
+      return e;
+    attr[ai] = true;
+  }
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kPThreads, kPSmemBytes)) != cudaSuccess)
+    return e;
+  if (per_sm <= 0) return cudaErrorNotSupported;
+  const int grid = std::min(sms * per_sm, 2 * ptiles(n));  // the widest level has 2 passes
+  UJob j;
+  j.sig = sig;
+  j.filt = filt;
+  j.out = out;
+  j.spec = spec;
+  j.n = n;
+  j.scale = scale;
+  void *args[] = {&j, &slot, (void *)&tw512, &status};
+  return cudaLaunchCooperativeKernel((const void *)kern, dim3(grid), dim3(kPThreads), args, kPSmemBytes, s);
 }
 
 }  // namespace convgpu

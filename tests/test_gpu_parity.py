@@ -90,6 +90,28 @@ def test_shared_filter_batches_against_fp32_oracle(gpu, n, how_many):
     assert gpu.device_status() == 0
 
 
+@pytest.mark.parametrize("n", [16, 32, 64])
+@pytest.mark.parametrize("per_signal", [False, True])
+def test_single_small_cube_one_launch(gpu, n, per_signal):
+    """One cube of N <= 64 runs as a single cooperative launch (the seven passes with grid
+    barriers between their dependency levels): the reference's criterion against the FP32
+    oracle, normalised and in place, one launch counted, device status clean."""
+    rng = np.random.default_rng(900 + n + per_signal)
+    sig = _c64(rng, (1, n, n, n))
+    filt = _c64(rng, (1, n, n, n) if per_signal else (n, n, n))
+    flags = gpu.FILTER_PER_SIGNAL if per_signal else 0
+    l0 = gpu.launch_count()
+    out = dev_conv(gpu, sig, filt, flags)
+    assert gpu.launch_count() - l0 == 1
+    assert snr_db(conv3d(sig, filt, "fp32", engine="pocketfft"), out) > SNR_DB
+    outn = dev_conv(gpu, sig, filt, flags | gpu.NORMALIZE, inplace=True)
+    np.testing.assert_allclose(outn, out / n ** 3, rtol=0, atol=1e-6 * np.abs(out).max() / n ** 3)
+    for _ in range(3):  # repeated launches reuse the barrier-slot ring
+        again = dev_conv(gpu, sig, filt, flags)
+    np.testing.assert_array_equal(again, out)
+    assert gpu.device_status() == 0
+
+
 @pytest.mark.slow
 def test_512_against_fp32_oracle(gpu):
     rng = np.random.default_rng(512)
