@@ -287,14 +287,14 @@ __global__ void __launch_bounds__(kPThreads, 3) k_persistent_queue(const UJob *_
 }
 
 // ------------------------------------------------------------------ small cubes, one launch
-// One convolution of a small cube (N <= 64) as a single cooperative launch: the seven
-// passes in their five dependency levels ({filter x, signal x}, {filter y, signal y},
-// fused z, y inverse, x inverse), each level's tiles spread over the grid, a grid barrier
-// between levels. A 64^3 cube is 2 MiB and stays in L2, so separate launches are bound by
+// One convolution of a small cube (N <= 64) as a single cooperative launch in three
+// dependency levels: x+y of the filter's and the signal's planes (each block holds its
+// planes in shared memory between the two transforms), the fused z pass, inverse y+x;
+// each level's items spread over the grid, a grid barrier between levels. A 64^3 cube is 2 MiB and stays in L2, so separate launches are bound by
 // launch gaps, not by HBM. The cooperative launch makes every block resident, so the
 // barrier cannot wait on a block that never runs; each wait is still bounded and one that
 // gives up sets kStatusQueueTimeout.
-// Barrier k (k = 1..4) of a launch waits until its counter reaches k * gridDim.x; every
+// Barrier k (k = 1, 2) of a launch waits until its counter reaches k * gridDim.x; every
 // launch uses its own counter slot, zeroed before use.
 __device__ __forceinline__ bool small_grid_barrier(unsigned *slot, unsigned target, unsigned *status) {
   __shared__ int s_ok;
@@ -318,21 +318,92 @@ __device__ __forceinline__ bool small_grid_barrier(unsigned *slot, unsigned targ
   return s_ok != 0;
 }
 
-// Pass i of dependency level lv (levels 0 and 1 have two passes, the others one).
-__device__ __forceinline__ int small_level_pass(int lv, int i) { return lv < 2 ? 2 * lv + i : lv + 2; }
+// Column n-slots of plane-column x of plane q in P consecutive N x N planes (row-major).
+struct PlaneCol {
+  int base, n_stride;
+  __device__ __forceinline__ int operator()(int n) const { return base + n * n_stride; }
+};
 
+// x then y transform of P consecutive N x N planes (P = 256 / (N * T) for N < 64, 1 for
+// N = 64, so that every round keeps all 256 threads busy), src -> dst, the planes held in
+// shared memory in between: x rows through a padded exchange buffer, y columns in place
+// (a warp's lanes are consecutive columns). INV: unnormalised backward transforms and
+// dst scaled by `scale`.
+template <int N, bool INV>
+__device__ __noinline__ void xy_planes_small(const float2 *src, float2 *dst, float scale, unsigned char *smraw,
+                                             const float2 *tw512) {
+  using S = PShape<N>;
+  constexpr int E = S::E, T = N / E;
+  constexpr int LINES = kPThreads / T;                 // rows (x) or columns (y) per round
+  constexpr int P = LINES >= N ? LINES / N : 1;        // planes per call
+  constexpr int ROUNDS = (P * N) / LINES;
+  constexpr int PITCH = row_pitch<N>();
+  static_assert(P * N % LINES == 0 && P * N * N * 8 + LINES * PITCH * 8 <= kPTwOffset, "plane buffers");
+  float2 *pl = reinterpret_cast<float2 *>(smraw);
+  float2 *ex = pl + P * N * N;
+  float2 *tw = reinterpret_cast<float2 *>(smraw + kPTwOffset);
+  for (int i = threadIdx.x; i < N; i += kPThreads) tw[i] = __ldg(tw512 + i * (512 / N));
+  for (int i = threadIdx.x; i < P * N * N; i += kPThreads) pl[i] = __ldcg(src + i);
+  __syncthreads();
+  float2 v[E];
+#pragma unroll 1
+  for (int rd = 0; rd < ROUNDS; ++rd) {  // x: row rr of the P planes
+    const int t = threadIdx.x % T, rl = threadIdx.x / T, rr = rd * LINES + rl;
+#pragma unroll
+    for (int e = 0; e < E; ++e) v[e] = pl[rr * N + t + e * T];
+    if (INV) swap_all(v);
+    fft_forward<N, E>(v, t, tw, ex, RowSlot<N>{rl * PITCH}, typename S::Plan{});
+    if (INV) swap_all(v);
+#pragma unroll
+    for (int e = 0; e < E; ++e) pl[rr * N + t + e * T] = v[e];
+    __syncthreads();  // the exchange buffer is reused by the next round
+  }
+#pragma unroll 1
+  for (int rd = 0; rd < ROUNDS; ++rd) {  // y: column x of plane q
+    const int c = threadIdx.x % LINES, t = threadIdx.x / LINES, gc = rd * LINES + c;
+    const int q = gc / N, x = gc % N;
+    const PlaneCol sidx{q * N * N + x, N};
+#pragma unroll
+    for (int e = 0; e < E; ++e) v[e] = pl[sidx(t + e * T)];
+    __syncthreads();  // every column's reads done before the in-place exchange
+    if (INV) swap_all(v);
+    fft_forward<N, E>(v, t, tw, pl, sidx, typename S::Plan{});
+    if (INV) swap_all(v);
+#pragma unroll
+    for (int e = 0; e < E; ++e) dst[sidx(t + e * T)] = make_float2(v[e].x * scale, v[e].y * scale);
+    __syncthreads();  // this round's columns read back before the next round's exchange
+  }
+}
+
+template <int N>
+constexpr int small_planes_per_item() {
+  return (kPThreads / (N / PShape<N>::E)) >= N ? (kPThreads / (N / PShape<N>::E)) / N : 1;
+}
+
+// Levels: 0 x+y of the filter's and the signal's planes, 1 the fused z pass (the filter's
+// z transform, product, inverse z), 2 inverse y+x of the output's planes.
 template <int N>
 __global__ void __launch_bounds__(kPThreads, 3) k_small_conv(UJob j, unsigned *slot, const float2 *tw512,
                                                              unsigned *status) {
   extern __shared__ __align__(128) unsigned char smraw[];
-  const int nt = ptiles(N);
-  for (int lv = 0; lv < 5; ++lv) {
-    const int npass = lv < 2 ? 2 : 1;
-    for (int w = blockIdx.x; w < npass * nt; w += gridDim.x) {
-      run_tile<N>(j, small_level_pass(lv, w / nt), w % nt, smraw, tw512);
-      __syncthreads();  // shared buffers are reused by the next tile
-    }
-    if (lv < 4 && !small_grid_barrier(slot, (unsigned)(lv + 1) * gridDim.x, status)) return;
+  constexpr int P = small_planes_per_item<N>(), NI = N / P;  // items per cube and level
+  const long long PL = (long long)P * N * N;                 // elements per item
+  for (int w = blockIdx.x; w < 2 * NI; w += gridDim.x) {
+    if (w < NI)
+      xy_planes_small<N, false>(j.filt + w * PL, j.spec + w * PL, 1.f, smraw, tw512);
+    else
+      xy_planes_small<N, false>(j.sig + (w - NI) * PL, j.out + (w - NI) * PL, 1.f, smraw, tw512);
+    __syncthreads();
+  }
+  if (!small_grid_barrier(slot, gridDim.x, status)) return;
+  for (int w = blockIdx.x; w < ptiles(N); w += gridDim.x) {
+    run_tile<N>(j, 4, w, smraw, tw512);
+    __syncthreads();
+  }
+  if (!small_grid_barrier(slot, 2u * gridDim.x, status)) return;
+  for (int w = blockIdx.x; w < NI; w += gridDim.x) {
+    xy_planes_small<N, true>(j.out + w * PL, j.out + w * PL, j.scale, smraw, tw512);
+    __syncthreads();
   }
 }
 
@@ -513,7 +584,8 @@ cudaError_t launch_small_conv(int n, const float2 *sig, const float2 *filt, floa
   if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kPThreads, kPSmemBytes)) != cudaSuccess)
     return e;
   if (per_sm <= 0) return cudaErrorNotSupported;
-  const int grid = std::min(sms * per_sm, 2 * ptiles(n));  // the widest level has 2 passes
+  const int widest = std::max(2 * n / (n == 64 ? 1 : (n == 32 ? 2 : 4)), ptiles(n));  // items of level 0 or 1
+  const int grid = std::min(sms * per_sm, widest);
   UJob j;
   j.sig = sig;
   j.filt = filt;
