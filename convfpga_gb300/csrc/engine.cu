@@ -368,8 +368,9 @@ static cudaError_t enqueue_conv_device(unsigned n, const float2 *sig, const floa
   const bool real = (flags & kFlagFilterReal) != 0;
   // One small cube (N <= 64, 2 MiB, L2-resident): the whole convolution in one cooperative
   // launch instead of seven launches separated by launch gaps.
-  if (how_many == 1 && tc == 0 && !real && n <= 64) {
-    const cudaError_t e = launch_small_conv((int)n, sig, filt, out, ws, scale, g.tw512, device_status_address(), s);
+  if (how_many == 1 && tc == 0 && n <= 64) {
+    const cudaError_t e =
+        launch_small_conv((int)n, sig, filt, out, ws, scale, real, g.tw512, device_status_address(), s);
     if (e == cudaSuccess) {
       count_launches(1);
       return cudaSuccess;

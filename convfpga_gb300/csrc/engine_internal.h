@@ -107,7 +107,7 @@ void release_uneven_plans();
 // One convolution of a small cube (N = 16, 32, 64) in one cooperative launch (persistent.cu);
 // spec: N^3 of workspace. cudaErrorNotSupported when it does not apply.
 cudaError_t launch_small_conv(int n, const float2 *sig, const float2 *filt, float2 *out, float2 *spec, float scale,
-                              const float2 *tw512, unsigned *status, cudaStream_t s);
+                              bool real, const float2 *tw512, unsigned *status, cudaStream_t s);
 
 // Returns and clears the device status word (kStatus* bits; ~0 if it cannot be read).
 unsigned int read_and_clear_device_status();

@@ -329,7 +329,9 @@ struct PlaneCol {
 // shared memory in between: x rows through a padded exchange buffer, y columns in place
 // (a warp's lanes are consecutive columns). INV: unnormalised backward transforms and
 // dst scaled by `scale`.
-template <int N, bool INV>
+// REAL: src holds floats (a real filter), widened to (x, 0) as they land, so the result is
+// bit-identical to that of the same values given as complex.
+template <int N, bool INV, bool REAL = false>
 __device__ __noinline__ void xy_planes_small(const float2 *src, float2 *dst, float scale, unsigned char *smraw,
                                              const float2 *tw512) {
   using S = PShape<N>;
@@ -343,7 +345,12 @@ __device__ __noinline__ void xy_planes_small(const float2 *src, float2 *dst, flo
   float2 *ex = pl + P * N * N;
   float2 *tw = reinterpret_cast<float2 *>(smraw + kPTwOffset);
   for (int i = threadIdx.x; i < N; i += kPThreads) tw[i] = __ldg(tw512 + i * (512 / N));
-  for (int i = threadIdx.x; i < P * N * N; i += kPThreads) pl[i] = __ldcg(src + i);
+  if constexpr (REAL) {
+    const float *rsrc = reinterpret_cast<const float *>(src);
+    for (int i = threadIdx.x; i < P * N * N; i += kPThreads) pl[i] = make_float2(__ldcg(rsrc + i), 0.f);
+  } else {
+    for (int i = threadIdx.x; i < P * N * N; i += kPThreads) pl[i] = __ldcg(src + i);
+  }
   __syncthreads();
   float2 v[E];
 #pragma unroll 1
@@ -382,14 +389,19 @@ constexpr int small_planes_per_item() {
 
 // Levels: 0 x+y of the filter's and the signal's planes, 1 the fused z pass (the filter's
 // z transform, product, inverse z), 2 inverse y+x of the output's planes.
+// real: j.filt holds N^3 floats (CONVGPU_FILTER_REAL).
 template <int N>
 __global__ void __launch_bounds__(kPThreads, 3) k_small_conv(UJob j, unsigned *slot, const float2 *tw512,
-                                                             unsigned *status) {
+                                                             unsigned *status, int real) {
   extern __shared__ __align__(128) unsigned char smraw[];
   constexpr int P = small_planes_per_item<N>(), NI = N / P;  // items per cube and level
   const long long PL = (long long)P * N * N;                 // elements per item
   for (int w = blockIdx.x; w < 2 * NI; w += gridDim.x) {
-    if (w < NI)
+    if (w < NI && real)
+      xy_planes_small<N, false, true>(
+          reinterpret_cast<const float2 *>(reinterpret_cast<const float *>(j.filt) + w * PL), j.spec + w * PL, 1.f,
+          smraw, tw512);
+    else if (w < NI)
       xy_planes_small<N, false>(j.filt + w * PL, j.spec + w * PL, 1.f, smraw, tw512);
     else
       xy_planes_small<N, false>(j.sig + (w - NI) * PL, j.out + (w - NI) * PL, 1.f, smraw, tw512);
@@ -553,10 +565,11 @@ void release_uneven_plans() {
 }
 
 // One convolution of an N^3 cube (N = 16, 32 or 64) in one cooperative launch: sig and
-// filt are N^3 complex64 each, spec is N^3 of workspace for the filter spectrum.
+// filt are N^3 complex64 each (filt N^3 floats with `real`), spec is N^3 of workspace for
+// the filter spectrum.
 // cudaErrorNotSupported for other N or when the grid cannot be co-resident.
 cudaError_t launch_small_conv(int n, const float2 *sig, const float2 *filt, float2 *out, float2 *spec, float scale,
-                              const float2 *tw512, unsigned *status, cudaStream_t s) {
+                              bool real, const float2 *tw512, unsigned *status, cudaStream_t s) {
   constexpr int kSlots = 1024;
   if (n != 16 && n != 32 && n != 64) return cudaErrorNotSupported;
   std::lock_guard<std::mutex> lk(g_pmu);
@@ -569,7 +582,7 @@ cudaError_t launch_small_conv(int n, const float2 *sig, const float2 *filt, floa
     if ((e = cudaMemsetAsync(g_small_slots, 0, kSlots * sizeof(unsigned), s)) != cudaSuccess) return e;
   }
   unsigned *slot = g_small_slots + (g_small_next++ % kSlots);
-  void (*kern)(UJob, unsigned *, const float2 *, unsigned *) =
+  void (*kern)(UJob, unsigned *, const float2 *, unsigned *, int) =
       n == 16 ? k_small_conv<16> : (n == 32 ? k_small_conv<32> : k_small_conv<64>);
   static bool attr[3] = {false, false, false};
   const int ai = n == 16 ? 0 : (n == 32 ? 1 : 2);
@@ -593,7 +606,8 @@ cudaError_t launch_small_conv(int n, const float2 *sig, const float2 *filt, floa
   j.spec = spec;
   j.n = n;
   j.scale = scale;
-  void *args[] = {&j, &slot, (void *)&tw512, &status};
+  int real_i = real ? 1 : 0;
+  void *args[] = {&j, &slot, (void *)&tw512, &status, &real_i};
   return cudaLaunchCooperativeKernel((const void *)kern, dim3(grid), dim3(kPThreads), args, kPSmemBytes, s);
 }
 
