@@ -13,8 +13,12 @@
 // Pass sequence of one convolution (per signal, 5 HBM passes; the reference streams
 // 3 phases with a DDR transpose inside each 3D FFT, host/src/convfpga.c:74-363):
 //   filter (shared):      x-fwd -> y-fwd -> z-fwd              (filter spectrum in workspace)
-//   filter (per signal):  x-fwd -> y-fwd                       (z done inside CONV_FZ)
+//   filter (per signal, or shared with one or two signals):
+//                         x-fwd -> y-fwd                       (z done inside CONV_FZ)
 //   signal:               x-fwd -> y-fwd -> z[fwd, (.)F, inv] -> y-inv -> x-inv(scale)
+// With the fused pass in the plan (N = 128, 256, 512), x-fwd -> y-fwd and y-inv -> x-inv
+// each run as one L2-staged launch. One cube of N <= 64 runs all of it in one cooperative
+// launch (persistent.cu: launch_small_conv).
 #include <cuda_runtime.h>
 
 #include <algorithm>
