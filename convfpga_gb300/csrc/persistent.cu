@@ -591,14 +591,24 @@ cudaError_t launch_small_conv(int n, const float2 *sig, const float2 *filt, floa
       return e;
     attr[ai] = true;
   }
-  int dev = 0, sms = 0, per_sm = 0;
+  // grid per size, computed once per device: the resident blocks, at most the widest level
+  static int grid_of[3] = {0, 0, 0}, grid_dev = -1;
+  int dev = 0;
   cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kPThreads, kPSmemBytes)) != cudaSuccess)
-    return e;
-  if (per_sm <= 0) return cudaErrorNotSupported;
-  const int widest = std::max(2 * n / (n == 64 ? 1 : (n == 32 ? 2 : 4)), ptiles(n));  // items of level 0 or 1
-  const int grid = std::min(sms * per_sm, widest);
+  if (dev != grid_dev) {
+    grid_of[0] = grid_of[1] = grid_of[2] = 0;
+    grid_dev = dev;
+  }
+  if (grid_of[ai] == 0) {
+    int sms = 0, per_sm = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kPThreads, kPSmemBytes)) != cudaSuccess)
+      return e;
+    if (per_sm <= 0) return cudaErrorNotSupported;
+    const int widest = std::max(2 * n / (n == 64 ? 1 : (n == 32 ? 2 : 4)), ptiles(n));  // items of level 0 or 1
+    grid_of[ai] = std::min(sms * per_sm, widest);
+  }
+  const int grid = grid_of[ai];
   UJob j;
   j.sig = sig;
   j.filt = filt;
