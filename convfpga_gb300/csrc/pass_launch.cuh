@@ -61,10 +61,14 @@ cudaError_t prepare_size();
 #ifdef CONVGPU_PASS_LAUNCH_IMPL
 
 template <class K>
-static cudaError_t set_smem_once(K kern, int smem, bool &done) {
-  if (done) return cudaSuccess;
+static cudaError_t set_smem_once(K kern, int smem, int &done) {
+  // `done` holds the device (+1) the limit was last set on: attributes belong to a
+  // device's context, so a process that moves to another device sets them again.
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (done == dev + 1) return cudaSuccess;
   const cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  if (e == cudaSuccess) done = true;
+  if (e == cudaSuccess) done = dev + 1;
   return e;
 }
 
@@ -76,7 +80,7 @@ static cudaError_t launch_gather(PassArgs a, int nvol, int nplanes, cudaStream_t
   constexpr int COLS = CONTIG ? S::XC : S::SC;
   constexpr int smem = pass_smem_bytes<N, E, COLS, CONTIG>();
   auto kern = k_axis_pass<N, E, COLS, CONTIG, OP, typename S::Plan>;
-  static bool done = false;
+  static int done = 0;
   cudaError_t e = set_smem_once(kern, smem, done);
   if (e != cudaSuccess) return e;
   a.groups_x = N / S::SC;
@@ -98,7 +102,7 @@ static cudaError_t launch_rows(const PassReq &r) {
   constexpr int E = S::E, XC = S::XC;
   constexpr int smem = tma_rows_smem_bytes<N, XC>();
   auto kern = k_rows_tma<N, E, XC, OP, typename S::Plan>;
-  static bool done = false;
+  static int done = 0;
   cudaError_t e = set_smem_once(kern, smem, done);
   if (e != cudaSuccess) return e;
   CUtensorMap m;
@@ -121,7 +125,7 @@ static cudaError_t launch_strided(const PassReq &r) {
   constexpr bool HAS_F = (OP == OP_CONV || OP == OP_CONV_FZ);
   constexpr int smem = tma_pass_smem_bytes<N, COLS, OP>();
   auto kern = k_strided_tma<N, E, COLS, OP, typename S::Plan>;
-  static bool done = false;
+  static int done = 0;
   cudaError_t e = set_smem_once(kern, smem, done);
   if (e != cudaSuccess) return e;
   PassArgs a = r.a;
@@ -191,7 +195,7 @@ static cudaError_t launch_rows_real(const PassReq &r) {
   constexpr int E = S::E, XC = S::XC;
   constexpr int smem = pass_smem_bytes<N, E, XC, true>();
   auto kern = k_rows_real<N, E, XC, typename S::Plan>;
-  static bool done = false;
+  static int done = 0;
   cudaError_t e = set_smem_once(kern, smem, done);
   if (e != cudaSuccess) return e;
   const long long blocks = (long long)r.nplanes * N / XC;

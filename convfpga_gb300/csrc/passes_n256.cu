@@ -22,7 +22,7 @@ static cudaError_t launch_tc256(int axis, PassArgs a, int nvol, cudaStream_t s) 
       const long long rows = (long long)nvol * N * N;
       if (!encode_rows_map(&m, a.src, N, rows, XC)) return cudaErrorNotSupported;
       auto kern = k_rows_tma_tc256<P, OP>;
-      static bool done = false;
+      static int done = 0;
       cudaError_t e = set_smem_once(kern, smem, done);
       if (e != cudaSuccess) return e;
       kern<<<(unsigned)(rows / XC), 256, smem, s>>>(m, a);
@@ -41,7 +41,7 @@ static cudaError_t launch_tc256(int axis, PassArgs a, int nvol, cudaStream_t s) 
     mfilt = msrc;
   }
   auto kern = k_strided_tma_tc256<P, OP>;
-  static bool done = false;
+  static int done = 0;
   cudaError_t e = set_smem_once(kern, smem, done);
   if (e != cudaSuccess) return e;
   a.vol_elems = 256LL * 256 * 256;
@@ -86,7 +86,7 @@ cudaError_t launch_xy256(const float2 *src, float2 *dst, int nplanes, bool inver
   CUtensorMap m;
   if (!encode_rows_map(&m, src, 256, (long long)nplanes * 256, kXyRows)) return cudaErrorNotSupported;
   auto kern = inverse ? k_xy256<true> : k_xy256<false>;
-  static bool done[2] = {false, false};
+  static int done[2] = {0, 0};
   cudaError_t e = set_smem_once(kern, kXySmem, done[inverse ? 1 : 0]);
   if (e != cudaSuccess) return e;
   static int max_clusters[2] = {0, 0};

@@ -584,21 +584,19 @@ cudaError_t launch_small_conv(int n, const float2 *sig, const float2 *filt, floa
   unsigned *slot = g_small_slots + (g_small_next++ % kSlots);
   void (*kern)(UJob, unsigned *, const float2 *, unsigned *, int) =
       n == 16 ? k_small_conv<16> : (n == 32 ? k_small_conv<32> : k_small_conv<64>);
-  static bool attr[3] = {false, false, false};
-  const int ai = n == 16 ? 0 : (n == 32 ? 1 : 2);
-  if (!attr[ai]) {
-    if ((e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kPSmemBytes)) != cudaSuccess)
-      return e;
-    attr[ai] = true;
-  }
-  // grid per size, computed once per device: the resident blocks, at most the widest level
+  // attribute and grid per size, set once per device: the grid is the resident blocks, at
+  // most the widest level
   static int grid_of[3] = {0, 0, 0}, grid_dev = -1;
+  const int ai = n == 16 ? 0 : (n == 32 ? 1 : 2);
   int dev = 0;
   cudaGetDevice(&dev);
   if (dev != grid_dev) {
     grid_of[0] = grid_of[1] = grid_of[2] = 0;
     grid_dev = dev;
   }
+  if (grid_of[ai] == 0 &&
+      (e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kPSmemBytes)) != cudaSuccess)
+    return e;
   if (grid_of[ai] == 0) {
     int sms = 0, per_sm = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);

@@ -18,7 +18,7 @@ static cudaError_t launch_tc05(int axis, PassArgs a, int nvol, cudaStream_t s) {
       const long long rows = (long long)nvol * N * N;
       if (!encode_rows_map(&m, a.src, N, rows, P)) return cudaErrorNotSupported;
       auto kern = k_tc05_256<P, OP, true>;
-      static bool done = false;
+      static int done = 0;
       cudaError_t e = set_smem_once(kern, T5Geom<P>::kSmem, done);
       if (e != cudaSuccess) return e;
       kern<<<(unsigned)(rows / P), T5Geom<P>::kThreads, T5Geom<P>::kSmem, s>>>(m, m, a, 0);
@@ -35,7 +35,7 @@ static cudaError_t launch_tc05(int axis, PassArgs a, int nvol, cudaStream_t s) {
     mfilt = msrc;
   }
   auto kern = k_tc05_256<P, OP, false>;
-  static bool done = false;
+  static int done = 0;
   cudaError_t e = set_smem_once(kern, T5Geom<P>::kSmem, done);
   if (e != cudaSuccess) return e;
   a.vol_elems = 256LL * 256 * 256;

@@ -56,7 +56,7 @@ static cudaError_t xy_l2_setup(long long max_planes, int &per_sm, int &sms, Scra
   const size_t cbytes = (2ull * max_planes + 2) * sizeof(unsigned);
   if (max_planes > 0 && (e = g_ctr.ensure(std::max<size_t>(cbytes, 64 << 10))) != cudaSuccess) return e;
   constexpr int smem = xyl2_smem<N>();
-  static bool done[4] = {false, false, false, false};
+  static int done[4] = {0, 0, 0, 0};
   if ((e = set_smem_once(k_xy_l2<N, false, false>, smem, done[0])) != cudaSuccess) return e;
   if ((e = set_smem_once(k_xy_l2<N, true, false>, smem, done[1])) != cudaSuccess) return e;
   if ((e = set_smem_once(k_xy_l2<N, false, true>, smem, done[2])) != cudaSuccess) return e;
