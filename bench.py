@@ -365,8 +365,11 @@ def _e2e(a, cg, sig, filt, shape, world, barrier):
     barrier()
     t0 = time.perf_counter()
     ok = True
+    call_s = []
     for _ in range(e2e_steps):
+        tc0 = time.perf_counter()
         t = cg.conv3d_host(N, hs.ptr, hf.ptr, ho.ptr, BATCH, e2e_flags)
+        call_s.append(time.perf_counter() - tc0)
         ok = ok and t.valid
     e2e_s = time.perf_counter() - t0
     assert ok, cg.last_error()
@@ -379,6 +382,10 @@ def _e2e(a, cg, sig, filt, shape, world, barrier):
     e2e = {"value": world * BATCH * e2e_steps / e2e_s, "unit": "conv/s",
            "h2d_bytes_per_step": 2 * vol * 8, "d2h_bytes_per_step": vol * 8,
            "api": "convgpu_conv3d_host (pinned host buffers)",
+           # the spread of the timed calls (the value above is their total): on a shared
+           # machine a few calls can wait on the host link
+           "call_ms": {"min": round(1e3 * min(call_s), 3), "median": round(1e3 * statistics.median(call_s), 3),
+                       "max": round(1e3 * max(call_s), 3)},
            "last_call_ms": {k: round(v, 3) for k, v in t.as_dict().items() if k != "valid"}}
     for b in (hs, hf, ho):
         b.free()
