@@ -5,11 +5,20 @@ Workload (the size the headline metric is quoted on): 4 convolutions of 256^3 co
 signals (re/im i.i.d. N(0,1)) with per-signal complex64 filters (re/im U[-1,1]), seeded
 synthetic data. One step = one batch of 4 convolutions through the library's C ABI.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--path fp32|tc]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--path both|fp32|tc]
 
-value      : convolutions/s with inputs resident in HBM (convgpu_conv3d_device), all ranks.
+value      : convolutions/s of the plain FP32 path with inputs resident in HBM
+             (convgpu_conv3d_device), all ranks.
+tc         : the same K steps on the same inputs through the tensor-core split path
+             (CONVGPU_TENSOR_SPLIT, TF32x3 on tcgen05): conv/s, its own roofline and pass
+             times, and tc_over_fp32 = its conv/s / the FP32 path's (default --path both).
+accuracy   : relative L2 and max-abs error of both paths against an FP64 FFT convolution
+             (numpy complex128) of one cube, checked after the timed region.
 e2e        : convolutions/s through convgpu_conv3d_host with pinned host buffers; every step
-             copies its inputs host->device and its outputs device->host.
+             copies its inputs host->device and its outputs device->host (tc.e2e: the same
+             with CONVGPU_TENSOR_SPLIT).
+e2e_dropin : a reference caller's call: fpgaf_conv3D_svm_batch on buffers from
+             fpgaf_complex_malloc (pageable), 128^3 x 8 with one shared real Gaussian filter.
 roofline   : the dominant pass kernel: algorithmic bytes per launch / mean launch time, timed
              with CUDA events on its stream during the timed region, against the measured HBM
              copy bandwidth of MEASURED_PEAKS.json.
@@ -44,7 +53,8 @@ def _args():
     p.add_argument("--steps", type=int, default=200)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    p.add_argument("--path", choices=["fp32", "tc"], default="fp32")
+    p.add_argument("--path", choices=["both", "fp32", "tc"], default="both",
+                   help="both: the FP32 path (value) and the tensor-core split path (tc) on the same inputs")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling runs)")
     p.add_argument("--batch", type=int, default=BATCH, help="cubes per step (profiling runs use 1)")
@@ -76,16 +86,34 @@ def _peaks():
         return 6800.0, "fallback"
 
 
+PATHS = {"fp32": "plain FP32 passes (autotuned plan)", "tc": "tcgen05 split-TF32 (TF32x3) passes",
+         "both": "plain FP32 passes (value) and tcgen05 split-TF32 passes (tc), same inputs"}
+
+
 def _config(path: str) -> dict:
     return {
         "workload": WORKLOAD,
         "n": N,
         "batch": BATCH,
         "filters": "per-signal",
-        "path": {"fp32": "plain FP32 per-axis passes", "tc": "tcgen05 split-TF32 (TF32x3) per-axis passes"}[path],
+        "path": PATHS[path],
         "normalised": False,
         "l2": "no flush: each step reads 1 GiB of inputs (> 129 MB L2)",
     }
+
+
+def _cpu_model() -> str:
+    """CPU model name of this host (lscpu), for the CPU baseline's record."""
+    try:
+        r = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10)
+        for line in r.stdout.splitlines():
+            if line.split(":")[0].strip() == "Model name":
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    import platform
+
+    return platform.processor() or platform.machine()
 
 
 # --------------------------------------------------------------------------- clocks
@@ -97,12 +125,14 @@ class ClockSampler:
     def __init__(self, device: int):
         self.device = device
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_bench_{device}.csv")
+        self.path = None
 
     def start(self):
         try:
-            os.makedirs(os.path.dirname(self.path), exist_ok=True)
-            self.fh = open(self.path, "w")
+            import tempfile
+
+            fd, self.path = tempfile.mkstemp(prefix=f"convgpu_clocks_{self.device}_", suffix=".csv")
+            self.fh = os.fdopen(fd, "w")
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "100",
                  "-i", str(self.device)], stdout=self.fh, stderr=subprocess.DEVNULL)
@@ -133,6 +163,10 @@ class ClockSampler:
                 for nm, v in zip(names, parts[5:9]):
                     if v.lower().startswith("active"):
                         reasons.add(nm)
+        try:
+            os.unlink(self.path)
+        except OSError:
+            pass
         if not sm:
             return None
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "samples": len(sm),
@@ -188,7 +222,7 @@ def cpu_baseline(budget_s: float = 20.0) -> dict:
     reps = max(2, min(5, int(budget_s / max(t1, 1e-3))))
     ts = [t1] + [_cpu_conv_sample(1.0, sig, filt, workers) for _ in range(reps - 1)]
     med = statistics.median(ts)
-    return {"value": 1.0 / med, "unit": "conv/s", "cores": workers, "kind": "port",
+    return {"value": 1.0 / med, "unit": "conv/s", "cores": workers, "kind": "port", "cpu_model": _cpu_model(),
             "sample": f"median of {len(ts)} single 256^3 convolutions (filter FFT + signal FFT + multiply + "
                       f"inverse FFT, pocketfft complex64, {workers} threads; FFTW3 unavailable - pocketfft "
                       f"stand-in), one of the 4 per step"}
@@ -221,13 +255,95 @@ def run_reference(a) -> None:
         "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 * tot / a.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
         "config": _config("fp32"),
-        "cpu_baseline": {"value": conv_s, "unit": "conv/s", "cores": workers, "kind": "port", "sample": sample},
+        "cpu_baseline": {"value": conv_s, "unit": "conv/s", "cores": workers, "kind": "port",
+                         "cpu_model": _cpu_model(), "sample": sample},
         "e2e": {"value": conv_s, "unit": "conv/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 
 
 # --------------------------------------------------------------------------- GPU side
+def _roofline(passes: dict, peak: float, peak_kind: str, arm: str = "fp32") -> dict:
+    """The dominant pass kernel's algorithmic bytes per launch over its mean launch time."""
+    dom_name, dom = max(passes.items(), key=lambda kv: kv[1]["ms"])
+    per_launch_bytes = dom["bytes"] / dom["launches"]
+    per_launch_s = dom["ms"] / dom["launches"] / 1e3
+    achieved = per_launch_bytes / per_launch_s / 1e9
+    return {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 4), "traffic": _read_traffic(dom_name if arm == "fp32" else f"{arm}/{dom_name}"),
+            "kernel": dom_name if arm == "fp32" else f"{arm}/{dom_name}",
+            "bytes_per_launch": per_launch_bytes,
+            "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
+            else "fallback 6.8 TB/s",
+            "share_of_step": round(dom["ms"] / sum(p["ms"] for p in passes.values()), 3)}
+
+
+def _passes_summary(passes: dict) -> dict:
+    return {k: {"ms_per_launch": round(v["ms"] / v["launches"], 4), "launches": v["launches"],
+                "gbs": round(v["bytes"] / (v["ms"] / 1e3) / 1e9, 1)} for k, v in passes.items()}
+
+
+def _time_arm(a, cg, flags, sig, filt, out, stream, world, barrier) -> dict:
+    """W warm-up steps, then K timed steps (CUDA events on the launching stream, barrier
+    and synchronize on both sides, max over ranks) with per-pass events recorded."""
+    import torch
+
+    def step():
+        cg.conv3d_device(N, sig, filt, out, BATCH, flags, stream)
+
+    for _ in range(a.warmup):
+        step()
+    torch.cuda.synchronize()
+    barrier()
+    torch.cuda.synchronize()
+    launches0 = cg.launch_count()
+    cg.pass_timing_start()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(a.steps):
+        step()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    torch.cuda.synchronize()
+    launches = cg.launch_count() - launches0
+    passes = cg.pass_timing_read()
+    cg.pass_timing_stop()
+    ms = ev0.elapsed_time(ev1)
+    if world > 1:
+        import torch.distributed as dist
+
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    return {"ms": ms, "passes": passes, "gpu_launches": launches, "status": cg.device_status()}
+
+
+def _fp64_errors(sig0, filt0, outs: dict) -> dict:
+    """Relative L2 and max-abs error of each path's output cube against the same
+    convolution in FP64: forward 3D FFTs of signal and filter in complex128, product,
+    unnormalised backward 3D FFT (numpy / scipy pocketfft, all host threads)."""
+    import numpy as np
+
+    try:
+        import scipy.fft as sfft
+
+        kw = {"workers": os.cpu_count() or 1}
+    except Exception:  # numpy alone
+        sfft, kw = np.fft, {}
+    s64 = sfft.fftn(sig0.astype(np.complex128), **kw)
+    s64 *= sfft.fftn(filt0.astype(np.complex128), **kw)
+    ref = sfft.ifftn(s64, norm="forward", **kw)
+    den = float(np.linalg.norm(ref.ravel()))
+    res = {}
+    for k, o in outs.items():
+        d = o.astype(np.complex128) - ref
+        res[k] = {"rel_l2": float(np.linalg.norm(d.ravel())) / den, "max_abs": float(np.abs(d).max()),
+                  "max_abs_ref": float(np.abs(ref).max())}
+    return res
+
+
 def run_ours(a) -> None:
     import torch
 
@@ -251,22 +367,17 @@ def run_ours(a) -> None:
     global BATCH
     BATCH = a.batch
     # The library's autotuner picks the plan for this size (shape variants, fused x+y
-    # pass or not) on this GPU before anything is timed.
+    # pass or not, tensor-core kernel family) on this GPU before anything is timed.
     if not replay:
         cg.autotune([N], write_cache=bool(a.plan_cache))
     plan = {k: cg.plan_variant(N, i) for i, k in enumerate(cg.PLAN_KINDS)}
-    flags = cg.FILTER_PER_SIGNAL | (cg.TENSOR_SPLIT if a.path == "tc" else 0)
     g = torch.Generator(device="cuda").manual_seed(1234 + rank)
     shape = (BATCH, N, N, N)
     sig = torch.complex(torch.randn(shape, device="cuda", generator=g),
                         torch.randn(shape, device="cuda", generator=g))
     filt = torch.complex(torch.rand(shape, device="cuda", generator=g) * 2 - 1,
                          torch.rand(shape, device="cuda", generator=g) * 2 - 1)
-    out = torch.empty_like(sig)
     stream = torch.cuda.current_stream()
-
-    def step():
-        cg.conv3d_device(N, sig, filt, out, BATCH, flags, stream)
 
     def barrier():
         if world > 1:
@@ -274,78 +385,71 @@ def run_ours(a) -> None:
 
             dist.barrier()
 
-    for _ in range(a.warmup):
-        step()
-    torch.cuda.synchronize()
-    barrier()
-    torch.cuda.synchronize()
-
+    arms = ["fp32", "tc"] if a.path == "both" else [a.path]
+    flags = {"fp32": cg.FILTER_PER_SIGNAL, "tc": cg.FILTER_PER_SIGNAL | cg.TENSOR_SPLIT}
+    outs = {k: torch.empty_like(sig) for k in arms}
     sampler = ClockSampler(local)
     sampler.start()
-    launches0 = cg.launch_count()
-    cg.pass_timing_start()
-    ev0 = torch.cuda.Event(enable_timing=True)
-    ev1 = torch.cuda.Event(enable_timing=True)
-    ev0.record(stream)
-    for _ in range(a.steps):
-        step()
-    ev1.record(stream)
-    torch.cuda.synchronize()
-    barrier()
-    torch.cuda.synchronize()
+    res = {k: _time_arm(a, cg, flags[k], sig, filt, outs[k], stream, world, barrier) for k in arms}
     clocks = sampler.stop()
-    gpu_launches = cg.launch_count() - launches0
-    passes = cg.pass_timing_read()
-    cg.pass_timing_stop()
-    ms = ev0.elapsed_time(ev1)
-    if world > 1:
-        import torch.distributed as dist
-
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    ms_step = ms / a.steps
-    value = world * BATCH * a.steps / (ms / 1e3)
 
     peak, peak_kind = _peaks()
-    dom_name, dom = max(passes.items(), key=lambda kv: kv[1]["ms"])
-    per_launch_bytes = dom["bytes"] / dom["launches"]
-    per_launch_s = dom["ms"] / dom["launches"] / 1e3
-    achieved = per_launch_bytes / per_launch_s / 1e9
-    traffic = _read_traffic(dom_name)
     model_bytes = BATCH * 136 * N ** 3  # per step: 48 N^3 per filter + 88 N^3 per signal
-    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                "frac": round(achieved / peak, 4), "traffic": traffic, "kernel": dom_name,
-                "bytes_per_launch": per_launch_bytes, "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"
-                if peak_kind == "measured" else "fallback 6.8 TB/s",
-                "share_of_step": round(dom["ms"] / sum(p["ms"] for p in passes.values()), 3)}
 
-    # e2e through the host-buffer C ABI entry point with pinned buffers.
-    e2e = _e2e(a, cg, sig, filt, shape, world, barrier) if not a.no_e2e else None
+    def arm_line(k):
+        r = res[k]
+        ms_step = r["ms"] / a.steps
+        return {"value": world * BATCH * a.steps / (r["ms"] / 1e3), "ms_per_step": ms_step,
+                "hbm_gbs_model": round(model_bytes / (ms_step / 1e3) / 1e9, 1),
+                "roofline": _roofline(r["passes"], peak, peak_kind, k), "passes": _passes_summary(r["passes"]),
+                "gpu_launches": r["gpu_launches"], "device_status": r["status"]}
+
+    lines = {k: arm_line(k) for k in arms}
+
+    # Accuracy of both paths on cube 0 of the last timed step, after the timed region.
+    accuracy = None
+    if rank == 0:
+        torch.cuda.synchronize()
+        accuracy = _fp64_errors(sig[0].cpu().numpy(), filt[0].cpu().numpy(),
+                                {k: outs[k][0].cpu().numpy() for k in arms})
+        accuracy["cube"] = "cube 0 of the batch, FP64 reference: numpy/scipy complex128 FFT convolution"
+    del outs
+
+    # e2e through the host-buffer C ABI entry point with pinned buffers, per arm.
+    e2e = {k: (_e2e(a, cg, sig, filt, shape, world, barrier, flags[k]) if not a.no_e2e else None) for k in arms}
+    dropin = _e2e_dropin(a, cg, world, barrier) if not a.no_e2e else None
 
     if rank != 0:
         return
+    main = arms[0]
     line = {
-        "metric": METRIC, "value": value, "unit": "conv/s", "n_gpus": world, "steps": a.steps,
-        "warmup": a.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "tf32x3" if a.path == "tc" else "f32",
+        "metric": METRIC, "value": lines[main]["value"], "unit": "conv/s", "n_gpus": world, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": lines[main]["ms_per_step"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "tf32x3" if main == "tc" else "f32",
         "data": "synthetic (seeded torch generator; signals N(0,1), filters U[-1,1])",
         "config": _config(a.path),
-        "hbm_gbs_model": round(model_bytes / (ms_step / 1e3) / 1e9, 1),
+        "hbm_gbs_model": lines[main]["hbm_gbs_model"],
         "plan": plan,
-        "roofline": roofline,
-        "passes": {k: {"ms_per_launch": round(v["ms"] / v["launches"], 4), "launches": v["launches"],
-                       "gbs": round(v["bytes"] / (v["ms"] / 1e3) / 1e9, 1)} for k, v in passes.items()},
-        "e2e": e2e,
-        "gpu_launches": gpu_launches,
+        "roofline": lines[main]["roofline"],
+        "passes": lines[main]["passes"],
+        "e2e": e2e[main],
+        "gpu_launches": lines[main]["gpu_launches"],
         "clocks": clocks,
+        "accuracy": accuracy,
+        "e2e_dropin": dropin,
     }
+    if "tc" in arms and main != "tc":
+        tc = dict(lines["tc"])
+        tc["dtype"] = "tf32x3"
+        tc["e2e"] = e2e["tc"]
+        tc["tc_over_fp32"] = round(tc["value"] / lines[main]["value"], 4)
+        line["tc"] = tc
     if world == 1 and not a.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline()
     print(json.dumps(line), flush=True)
 
 
-def _e2e(a, cg, sig, filt, shape, world, barrier):
+def _e2e(a, cg, sig, filt, shape, world, barrier, e2e_flags):
     import torch
 
     vol = BATCH * N ** 3
@@ -355,7 +459,6 @@ def _e2e(a, cg, sig, filt, shape, world, barrier):
     sig_h, filt_h, out_h = hs.array(shape), hf.array(shape), ho.array(shape)
     sig_h[...] = sig.cpu().numpy()
     filt_h[...] = filt.cpu().numpy()
-    e2e_flags = cg.FILTER_PER_SIGNAL
     for _ in range(2):
         t = cg.conv3d_host(N, hs.ptr, hf.ptr, ho.ptr, BATCH, e2e_flags)
         assert t.valid, cg.last_error()
@@ -381,7 +484,8 @@ def _e2e(a, cg, sig, filt, shape, world, barrier):
         e2e_s = float(tt.item())
     e2e = {"value": world * BATCH * e2e_steps / e2e_s, "unit": "conv/s",
            "h2d_bytes_per_step": 2 * vol * 8, "d2h_bytes_per_step": vol * 8,
-           "api": "convgpu_conv3d_host (pinned host buffers)",
+           "api": "convgpu_conv3d_host (pinned host buffers)"
+                  + (", CONVGPU_TENSOR_SPLIT" if e2e_flags & cg.TENSOR_SPLIT else ""),
            # the spread of the timed calls (the value above is their total): on a shared
            # machine a few calls can wait on the host link
            "call_ms": {"min": round(1e3 * min(call_s), 3), "median": round(1e3 * statistics.median(call_s), 3),
@@ -390,6 +494,59 @@ def _e2e(a, cg, sig, filt, shape, world, barrier):
     for b in (hs, hf, ho):
         b.free()
     return e2e
+
+
+def _e2e_dropin(a, cg, world, barrier) -> dict:
+    """What a reference caller gets: src/main.cpp:64-74 of pc2/ConvFPGA allocates its
+    buffers with fpgaf_complex_malloc (pageable host memory) and calls
+    fpgaf_conv3D_svm_batch. Workload: 128^3 x 8 signals (U[-1,1]) with one shared real
+    periodic Gaussian filter (sigma 4) stored as complex with zero imaginary parts, as the
+    reference's API takes it. Each call copies 8 signals and the filter up and 8 outputs
+    down; the library transforms the filter on every call, as the reference does."""
+    import numpy as np
+    import torch
+
+    n, b = 128, 8
+    vol = n ** 3
+    hs, hf, ho = (cg.ComplexMalloc.alloc(c * vol * 8) for c in (b, 1, b))
+    rng = np.random.default_rng(7)
+    sa, fa = hs.array((b, n, n, n)), hf.array((n, n, n))
+    sa.real = rng.uniform(-1, 1, (b, n, n, n)).astype(np.float32)
+    sa.imag = rng.uniform(-1, 1, (b, n, n, n)).astype(np.float32)
+    d = np.minimum(np.arange(n), n - np.arange(n)).astype(np.float64) ** 2
+    fa[...] = np.exp(-(d[:, None, None] + d[None, :, None] + d[None, None, :]) / (2 * 16.0)).astype(np.complex64)
+    ho.array((b, n, n, n))[...] = 0
+    for _ in range(2):
+        t = cg.fpgaf_conv3D_svm_batch(n, hs.ptr, hf.ptr, ho.ptr, b)
+        assert t.valid, cg.last_error()
+    calls = max(3, min(a.steps, 30))
+    barrier()
+    call_s = []
+    ok = True
+    t0 = time.perf_counter()
+    for _ in range(calls):
+        tc0 = time.perf_counter()
+        t = cg.fpgaf_conv3D_svm_batch(n, hs.ptr, hf.ptr, ho.ptr, b)
+        call_s.append(time.perf_counter() - tc0)
+        ok = ok and t.valid
+    tot = time.perf_counter() - t0
+    assert ok, cg.last_error()
+    if world > 1:
+        import torch.distributed as dist
+
+        tt = torch.tensor([tot], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        tot = float(tt.item())
+    res = {"value": world * b * calls / tot, "unit": "conv/s", "h2d_bytes_per_step": (b + 1) * vol * 8,
+           "d2h_bytes_per_step": b * vol * 8,
+           "api": "fpgaf_conv3D_svm_batch on fpgaf_complex_malloc buffers (pageable)",
+           "workload": "128^3 complex64 x8, one shared real Gaussian filter (sigma 4) as complex",
+           "call_ms": {"min": round(1e3 * min(call_s), 3), "median": round(1e3 * statistics.median(call_s), 3),
+                       "max": round(1e3 * max(call_s), 3)},
+           "last_call_ms": {k: round(v, 3) for k, v in t.as_dict().items() if k != "valid"}}
+    for h in (hs, hf, ho):
+        h.free()
+    return res
 
 
 def run_uneven(a) -> None:
@@ -538,7 +695,8 @@ def run_configs(a) -> None:
 
 
 def _read_traffic(kernel: str):
-    """DRAM bytes per launch of the dominant kernel from the committed ncu summary, if any."""
+    """DRAM bytes per launch of the dominant kernel from the committed ncu summary, if any
+    (keys of the tensor-core path's kernels start with "tc/")."""
     try:
         with open(os.path.join(ROOT, "profiles", "dram_traffic.json")) as f:
             d = json.load(f)

@@ -336,6 +336,36 @@ def synchronize() -> None:
 
 
 @dataclass
+class ComplexMalloc:
+    """Host block from fpgaf_complex_malloc (64-byte aligned, pageable), the buffers a
+    reference caller hands to the conv entry points (src/main.cpp:64-74 of pc2/ConvFPGA);
+    released with the C library's free(), as the reference's callers do."""
+
+    ptr: int
+    nbytes: int
+
+    @classmethod
+    def alloc(cls, nbytes: int) -> "ComplexMalloc":
+        p = load_library().fpgaf_complex_malloc(nbytes)
+        if not p:
+            raise ConvGpuError(f"fpgaf_complex_malloc({nbytes}) returned NULL")
+        return cls(int(p), nbytes)
+
+    def array(self, shape) -> np.ndarray:
+        count = int(np.prod(shape))
+        buf = (ctypes.c_char * (count * 8)).from_address(self.ptr)
+        return np.frombuffer(buf, dtype=np.complex64, count=count).reshape(shape)
+
+    def free(self) -> None:
+        if self.ptr:
+            libc = ctypes.CDLL(None)
+            libc.free.argtypes = [ctypes.c_void_p]
+            libc.free.restype = None
+            libc.free(self.ptr)
+            self.ptr = 0
+
+
+@dataclass
 class PinnedBuffer:
     """Page-locked host block from convgpu_host_alloc, viewed as complex64."""
 

@@ -24,7 +24,7 @@ def test_reference_arm_prints_one_contract_line():
     assert line["warmup"] == 3  # fewer warm-up steps than 3 are raised to 3
     cb = line["cpu_baseline"]
     assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["value"] == line["value"]
-    assert "sample" in cb
+    assert "sample" in cb and cb["cpu_model"]
     assert line["e2e"] == {"value": line["value"], "unit": "conv/s", "h2d_bytes_per_step": 0,
                            "d2h_bytes_per_step": 0}
     assert "workload" in line["config"]
