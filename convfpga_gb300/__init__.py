@@ -65,6 +65,8 @@ EXPORTED_SYMBOLS = (
     "convgpu_device_status",
     "convgpu_autotune",
     "convgpu_plan_variant",
+    "convgpu_debug_dependency_wait_limit",
+    "convgpu_debug_fail_allocations",
     "convgpu_last_error",
 )
 
@@ -156,6 +158,10 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
     lib.convgpu_autotune.restype = ctypes.c_int
     lib.convgpu_plan_variant.argtypes = [ctypes.c_uint, ctypes.c_int, ctypes.c_int]
     lib.convgpu_plan_variant.restype = ctypes.c_int
+    lib.convgpu_debug_dependency_wait_limit.argtypes = [ctypes.c_int]
+    lib.convgpu_debug_dependency_wait_limit.restype = ctypes.c_int
+    lib.convgpu_debug_fail_allocations.argtypes = [ctypes.c_uint]
+    lib.convgpu_debug_fail_allocations.restype = ctypes.c_int
     lib.convgpu_last_error.argtypes = []
     lib.convgpu_last_error.restype = ctypes.c_char_p
     if path is None:
@@ -329,6 +335,16 @@ def device_status() -> int:
     v = ctypes.c_uint(0)
     _check(load_library().convgpu_device_status(ctypes.byref(v)), "convgpu_device_status")
     return int(v.value)
+
+
+def debug_dependency_wait_limit(probes: int) -> None:
+    """Testing hook: dependency waits give up after `probes` probes (< 0: default)."""
+    _check(load_library().convgpu_debug_dependency_wait_limit(probes), "convgpu_debug_dependency_wait_limit")
+
+
+def debug_fail_allocations(count: int) -> None:
+    """Testing hook: the next `count` device-buffer allocations fail as out of memory."""
+    _check(load_library().convgpu_debug_fail_allocations(count), "convgpu_debug_fail_allocations")
 
 
 def synchronize() -> None:

@@ -47,5 +47,7 @@ int bridge_sync();
 int bridge_autotune(const unsigned *sizes, unsigned count, int write_cache);
 int bridge_plan_variant(unsigned n, int kind, int set_to);
 int bridge_device_status(unsigned *status);
+int bridge_debug_wait_limit(int probes);
+int bridge_debug_fail_allocations(unsigned count);
 
 }  // namespace convgpu

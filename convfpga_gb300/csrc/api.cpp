@@ -106,6 +106,10 @@ int convgpu_plan_variant(unsigned N, int kind, int set_to) { return convgpu::bri
 
 int convgpu_device_status(unsigned *status) { return convgpu::bridge_device_status(status); }
 
+int convgpu_debug_dependency_wait_limit(int probes) { return convgpu::bridge_debug_wait_limit(probes); }
+
+int convgpu_debug_fail_allocations(unsigned count) { return convgpu::bridge_debug_fail_allocations(count); }
+
 const char *convgpu_last_error(void) { return convgpu::bridge_last_error(); }
 
 }  // extern "C"

@@ -69,6 +69,11 @@ static int cuda_fail(cudaError_t e, const char *what) {
 
 static bool valid_n(unsigned n) { return n >= 16 && n <= 512 && (n & (n - 1)) == 0; }
 
+// Allocations still to fail on purpose (testing hook, fail_next_allocations).
+static std::atomic<unsigned> g_fail_allocs{0};
+
+void fail_next_allocations(unsigned count) { g_fail_allocs.store(count); }
+
 // Grow-only device buffer. Growing synchronises the device first, so work still in
 // flight on the old block never sees it freed.
 struct DevBuf {
@@ -82,6 +87,8 @@ struct DevBuf {
       p = nullptr;
       bytes = 0;
     }
+    for (unsigned f = g_fail_allocs.load(); f > 0;)
+      if (g_fail_allocs.compare_exchange_weak(f, f - 1)) return cudaErrorMemoryAllocation;
     cudaError_t e = cudaMalloc(&p, b);
     if (e == cudaSuccess) bytes = b;
     return e;
@@ -116,8 +123,49 @@ struct Engine {
   DevBuf hio[3];       // host API: signal chunk buffers
   DevBuf hfio[3];      // host API: per-signal filter chunk buffers
   std::string plan_path;
+  // End of the last call's work (CallOrder): the stream it was enqueued on and an event.
+  cudaEvent_t last_done = nullptr;
+  cudaStream_t last_stream = nullptr;
+  bool last_valid = false;
 };
 static Engine g;
+
+// ------------------------------------------------------------------ cross-stream order
+// The workspace, the fused x+y pass's scratch ring and counters, and the uneven batch's
+// cached plans are shared by every call, so calls enqueued on different streams are
+// ordered on the GPU: a call on stream s first waits for the previous call's work when
+// that went to another stream, and records its own end for the next call. Calls on one
+// stream are ordered by the stream already, at no cost. A stream that is being captured
+// into a graph is left alone (the graph cannot wait on work outside it): a graph that
+// contains a call must not run while another call is in flight.
+static bool capturing(cudaStream_t s) {
+  cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &st) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return st != cudaStreamCaptureStatusNone;
+}
+
+struct CallOrder {
+  cudaStream_t s;
+  bool active;
+  explicit CallOrder(cudaStream_t st) : s(st), active(!capturing(st)) {
+    if (active && g.last_valid && g.last_stream != s) cudaStreamWaitEvent(s, g.last_done, 0);
+  }
+  // Records even when the call failed partway: the event then follows what was enqueued.
+  ~CallOrder() {
+    if (!active) return;
+    if (!g.last_done && cudaEventCreateWithFlags(&g.last_done, cudaEventDisableTiming) != cudaSuccess) {
+      g.last_done = nullptr;
+      return;
+    }
+    if (cudaEventRecord(g.last_done, s) == cudaSuccess) {
+      g.last_stream = s;
+      g.last_valid = true;
+    }
+  }
+};
 static void load_plan_cache(const std::string &path);
 
 static cudaError_t upload_twiddles(float2 **dst) {
@@ -153,6 +201,9 @@ static void teardown_locked() {
   if (g.sh2d) cudaStreamDestroy(g.sh2d);
   if (g.sd2h) cudaStreamDestroy(g.sd2h);
   g.sc = g.sh2d = g.sd2h = nullptr;
+  if (g.last_done) cudaEventDestroy(g.last_done);
+  g.last_done = nullptr;
+  g.last_valid = false;
   g.init = false;
 }
 
@@ -469,6 +520,7 @@ int bridge_conv_device(unsigned n, const void *d_sig, const void *d_filt, void *
   if (rc) return rc;
   cudaError_t e = g.ws.ensure(workspace_bytes_for(n, how_many, flags));
   if (e != cudaSuccess) return cuda_fail(e, "workspace");
+  CallOrder order((cudaStream_t)stream);
   e = enqueue_conv_device(n, (const float2 *)d_sig, (const float2 *)d_filt, (float2 *)d_out, how_many, flags,
                           (float2 *)g.ws.p, (cudaStream_t)stream);
   if (e != cudaSuccess) return cuda_fail(e, "launch");
@@ -484,9 +536,45 @@ int bridge_filter_spectrum_device(unsigned n, const void *d_filt, void *d_spec, 
   std::lock_guard<std::recursive_mutex> lk(g.mu);
   int rc = ensure_init_locked();
   if (rc) return rc;
+  CallOrder order((cudaStream_t)stream);
   cudaError_t e = enqueue_filter(n, (const float2 *)d_filt, (float2 *)d_spec, count, false, (cudaStream_t)stream);
   if (e != cudaSuccess) return cuda_fail(e, "launch");
   return 0;
+}
+
+// Checks an uneven batch's descriptors before anything runs: every size supported; every
+// cube's element range addressable from its base pointer (no wrap of the 64-bit address);
+// a job's output either is its own signal (in place) or does not overlap it; and no two
+// jobs' outputs overlap (their passes would overwrite each other's data). Returns "" or
+// the reason.
+static std::string check_jobs(const UnevenJob *jobs, unsigned njobs, const void *d_sig, const void *d_filt,
+                              const void *d_out) {
+  const unsigned long long kMax = ~0ull;
+  std::vector<std::pair<unsigned long long, unsigned>> outs(njobs);
+  for (unsigned j = 0; j < njobs; ++j) {
+    const UnevenJob &jb = jobs[j];
+    if (!valid_n(jb.n)) return "job " + std::to_string(j) + ": size " + std::to_string(jb.n) + " not supported";
+    const unsigned long long v = (unsigned long long)jb.n * jb.n * jb.n;
+    const void *base[3] = {d_sig, d_filt, d_out};
+    const unsigned long long off[3] = {jb.sig_off, jb.filt_off, jb.out_off};
+    for (int k = 0; k < 3; ++k) {
+      // byte end = base + (off + v) * 8 must not pass the end of the address space
+      const unsigned long long b = (unsigned long long)reinterpret_cast<uintptr_t>(base[k]);
+      if (off[k] > kMax / 8 - v || (off[k] + v) * 8 > kMax - b)
+        return "job " + std::to_string(j) + ": offset " + std::to_string(off[k]) + " lies past the address space";
+    }
+    if (d_sig == d_out && jb.sig_off != jb.out_off && jb.sig_off < jb.out_off + v && jb.out_off < jb.sig_off + v)
+      return "job " + std::to_string(j) + ": output partly overlaps its own signal";
+    outs[j] = {jb.out_off, j};
+  }
+  std::sort(outs.begin(), outs.end());
+  for (unsigned i = 1; i < njobs; ++i) {
+    const UnevenJob &a = jobs[outs[i - 1].second];
+    if (outs[i - 1].first + (unsigned long long)a.n * a.n * a.n > outs[i].first)
+      return "outputs of jobs " + std::to_string(outs[i - 1].second) + " and " + std::to_string(outs[i].second) +
+             " overlap";
+  }
+  return "";
 }
 
 int bridge_conv_uneven_device(const UnevenJob *jobs, unsigned njobs, const void *d_sig, const void *d_filt,
@@ -495,11 +583,11 @@ int bridge_conv_uneven_device(const UnevenJob *jobs, unsigned njobs, const void 
     set_err("invalid arguments");
     return kErrInval;
   }
-  for (unsigned j = 0; j < njobs; ++j)
-    if (!valid_n(jobs[j].n)) {
-      set_err("job with unsupported size");
-      return kErrInval;
-    }
+  const std::string bad = check_jobs(jobs, njobs, d_sig, d_filt, d_out);
+  if (!bad.empty()) {
+    set_err(bad);
+    return kErrInval;
+  }
   if (flags & kFlagFilterReal) {
     set_err("CONVGPU_FILTER_REAL is not supported by the uneven-batch entry point");
     return kErrUnsupported;
@@ -510,6 +598,7 @@ int bridge_conv_uneven_device(const UnevenJob *jobs, unsigned njobs, const void 
   const bool normalize = (flags & kFlagNormalize) != 0;
   if (!(flags & (kFlagUnevenPerJob | kFlagTensorSplit | kFlagTensorBf16x3 | kFlagFilterIsSpectrum))) {
     std::string err;
+    CallOrder order((cudaStream_t)stream);
     if (flags & kFlagUnevenQueue) {
       unsigned *status = device_status_address();
       if (!status) return cuda_fail(cudaErrorInvalidSymbol, "device status word");
@@ -529,6 +618,7 @@ int bridge_conv_uneven_device(const UnevenJob *jobs, unsigned njobs, const void 
   for (unsigned j = 0; j < njobs; ++j) need = std::max(need, workspace_bytes_for(jobs[j].n, 1, flags & ~kFlagPerSignalFilter));
   cudaError_t e = g.ws.ensure(need);
   if (e != cudaSuccess) return cuda_fail(e, "workspace");
+  CallOrder order((cudaStream_t)stream);
   for (unsigned j = 0; j < njobs; ++j) {
     const float2 *s = (const float2 *)d_sig + jobs[j].sig_off;
     const float2 *f = (const float2 *)d_filt + jobs[j].filt_off;
@@ -730,6 +820,7 @@ Timing bridge_conv_host(unsigned n, const void *sig, const void *filt, void *out
   std::lock_guard<std::recursive_mutex> lk(g.mu);
   if (ensure_init_locked() != 0) return t;
   (void)mode;
+  CallOrder order(g.sc);  // compute waits for device calls still in flight on other streams
 
   const bool per_signal = (flags & kFlagPerSignalFilter) != 0;
   const bool real = (flags & kFlagFilterReal) != 0;  // filt holds N^3 floats per filter
@@ -954,6 +1045,7 @@ int bridge_autotune(const unsigned *sizes, unsigned count, int write_cache) {
   int rc = ensure_init_locked();
   if (rc) return rc;
   cudaStream_t s = g.sc;
+  CallOrder order(s);
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
@@ -1141,6 +1233,20 @@ int bridge_device_status(unsigned *status) {
   cudaError_t e = cudaDeviceSynchronize();
   if (e != cudaSuccess) return cuda_fail(e, "synchronize");
   *status = read_and_clear_device_status();
+  return 0;
+}
+
+int bridge_debug_wait_limit(int probes) {
+  std::lock_guard<std::recursive_mutex> lk(g.mu);
+  int rc = ensure_init_locked();
+  if (rc) return rc;
+  const cudaError_t e = set_dependency_wait_limit(probes);
+  if (e != cudaSuccess) return cuda_fail(e, "dependency wait limit");
+  return 0;
+}
+
+int bridge_debug_fail_allocations(unsigned count) {
+  fail_next_allocations(count);
   return 0;
 }
 

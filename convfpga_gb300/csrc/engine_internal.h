@@ -111,6 +111,12 @@ cudaError_t launch_small_conv(int n, const float2 *sig, const float2 *filt, floa
 
 // Returns and clears the device status word (kStatus* bits; ~0 if it cannot be read).
 unsigned int read_and_clear_device_status();
+// Testing hook: every dependency wait (counters advanced by other CTAs) gives up after
+// `probes` probes; probes < 0 restores each wait's own limit. Waits for the device first.
+cudaError_t set_dependency_wait_limit(int probes);
+// Testing hook: the next `count` allocations of the runtime's grow-only device buffers
+// fail as out of memory.
+void fail_next_allocations(unsigned count);
 
 // Checks that this library's kernel image loads on the current device.
 cudaError_t probe_kernel_image();

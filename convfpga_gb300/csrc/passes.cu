@@ -18,7 +18,10 @@
 
 namespace convgpu {
 
-__device__ unsigned int g_device_status = 0;
+// Word 0: the device status word (kStatus* bits, OR-ed in by kernels whose bounded wait
+// gave up). Word 1: the dependency-wait limit that tests may lower (tma.cuh:
+// dep_wait_limit; 0 = every wait's own limit). Kernels get the address of word 0.
+__device__ unsigned int g_device_words[2] = {0u, 0u};
 
 extern template cudaError_t launch_size<16>(const PassReq &);
 extern template cudaError_t launch_size<32>(const PassReq &);
@@ -125,7 +128,7 @@ unsigned int *device_status_address() {
   unsigned int *p = cache[dev].load();
   if (!p) {
     void *q = nullptr;
-    if (cudaGetSymbolAddress(&q, g_device_status) != cudaSuccess) return nullptr;
+    if (cudaGetSymbolAddress(&q, g_device_words) != cudaSuccess) return nullptr;
     p = static_cast<unsigned int *>(q);
     cache[dev].store(p);
   }
@@ -134,10 +137,19 @@ unsigned int *device_status_address() {
 
 unsigned int read_and_clear_device_status() {
   unsigned int v = 0;
-  if (cudaMemcpyFromSymbol(&v, g_device_status, sizeof(v)) != cudaSuccess) return ~0u;
+  if (cudaMemcpyFromSymbol(&v, g_device_words, sizeof(v)) != cudaSuccess) return ~0u;
   const unsigned int zero = 0;
-  cudaMemcpyToSymbol(g_device_status, &zero, sizeof(zero));
+  cudaMemcpyToSymbol(g_device_words, &zero, sizeof(zero));
   return v;
+}
+
+cudaError_t set_dependency_wait_limit(int probes) {
+  const unsigned int v = probes < 0 ? 0u : (unsigned int)probes + 1u;
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) return e;
+  e = cudaMemcpyToSymbol(g_device_words, &v, sizeof(v), sizeof(unsigned int));
+  if (e != cudaSuccess) return e;
+  return cudaDeviceSynchronize();
 }
 
 // ------------------------------------------------------------------ plan table

@@ -12,8 +12,9 @@
 // passes p depends on (for the same job) is counted done. Items are dequeued in level
 // order and a CTA waits only on items dequeued before its own, by CTAs that are already
 // running, so the launch cannot deadlock whatever number of CTAs is resident. Waits are
-// bounded: after kSpinLimit probes the CTA records kStatusQueueTimeout in the device
-// status word, skips the tile and counts it done, so the launch always terminates.
+// bounded: after kSpinLimit probes (fewer when a test lowers the dependency-wait limit,
+// tma.cuh: dep_wait_limit) the CTA records kStatusQueueTimeout in the device status word,
+// skips the tile and counts it done, so the launch always terminates.
 //
 // Data written by one CTA is read by others in later passes, so every global load of
 // cube data here uses ld.global.cg (L2, not the incoherent L1); a CTA publishes a finished
@@ -235,6 +236,7 @@ __global__ void __launch_bounds__(kPThreads, 3) k_persistent_queue(const UJob *_
                                                                 unsigned *status) {
   extern __shared__ __align__(128) unsigned char smraw[];
   __shared__ int s_item, s_ok;
+  const uint32_t spin = dep_wait_limit(status, kSpinLimit);
   for (;;) {
     if (threadIdx.x == 0) s_item = atomicAdd(head, 1);
     __syncthreads();
@@ -250,14 +252,17 @@ __global__ void __launch_bounds__(kPThreads, 3) k_persistent_queue(const UJob *_
         const int d = pass_dep(pass, k);
         if (d < 0) continue;
         const int *cnt = counters + job * kPasses + d;
-        uint32_t spins = 0;
-        while (ld_acquire(cnt) < target) {
-          if (++spins > kSpinLimit) {
-            ok = 0;
-            atomicOr(status, kStatusQueueTimeout);
+        bool done = false;
+        for (uint32_t i = 0; i < spin; ++i) {
+          if (ld_acquire(cnt) >= target) {
+            done = true;
             break;
           }
           __nanosleep(64);
+        }
+        if (!done) {
+          ok = 0;
+          atomicOr(status, kStatusQueueTimeout);
         }
       }
       s_ok = ok;
@@ -302,16 +307,16 @@ __device__ __forceinline__ bool small_grid_barrier(unsigned *slot, unsigned targ
   if (threadIdx.x == 0) {
     __threadfence();  // ... and visible device-wide before the arrival
     atomicAdd(slot, 1u);
-    int ok = 1;
-    uint32_t spins = 0;
-    while ((unsigned)ld_acquire(reinterpret_cast<const int *>(slot)) < target) {
-      if (++spins > kSpinLimit) {
-        ok = 0;
-        if (status) atomicOr(status, kStatusQueueTimeout);
+    int ok = 0;
+    const uint32_t spin = dep_wait_limit(status, kSpinLimit);
+    for (uint32_t i = 0; i < spin; ++i) {
+      if ((unsigned)ld_acquire(reinterpret_cast<const int *>(slot)) >= target) {
+        ok = 1;
         break;
       }
       __nanosleep(32);
     }
+    if (!ok && status) atomicOr(status, kStatusQueueTimeout);
     s_ok = ok;
   }
   __syncthreads();

@@ -16,6 +16,18 @@ namespace convgpu {
 constexpr unsigned kStatusTmaTimeout = 1u;
 constexpr uint32_t kWaitLimit = 1u << 22;
 
+// The device status word is followed by a second word, the dependency-wait limit: 0
+// keeps each dependency wait's own probe limit; v > 0 limits every dependency wait (on a
+// counter another CTA advances: plane dependencies of the L2-staged pass, the uneven work
+// queue, the small-cube grid barriers) to v - 1 probes, so v = 1 makes them give up at
+// once. It exists for tests of the failure path; waits for copies or MMAs in flight
+// (mbarrier waits) never read it.
+__device__ __forceinline__ uint32_t dep_wait_limit(const unsigned *status, uint32_t dflt) {
+  if (!status) return dflt;
+  const unsigned v = *reinterpret_cast<const volatile unsigned *>(status + 1);
+  return v ? v - 1u : dflt;
+}
+
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }

@@ -57,10 +57,10 @@ __device__ __forceinline__ void red_relaxed_add_u32(unsigned *p, unsigned v) {
   asm volatile("red.relaxed.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
-// Polls *p until it reaches `target` (bounded, with back-off). Thread 0 only.
-__device__ __forceinline__ bool wait_count(const unsigned *p, unsigned target) {
+// Polls *p until it reaches `target`, at most `limit` probes with back-off. Thread 0 only.
+__device__ __forceinline__ bool wait_count(const unsigned *p, unsigned target, uint32_t limit) {
   unsigned ns = 32;
-  for (uint32_t i = 0; i < kXyL2Spin; ++i) {
+  for (uint32_t i = 0; i < limit; ++i) {
     if (ld_acquire_u32(p) >= target) return true;
     __nanosleep(ns);
     if (ns < 512) ns <<= 1;
@@ -255,6 +255,7 @@ __global__ void __launch_bounds__(kXyL2Threads, 8) k_xy_l2(const __grid_constant
   const int lag = (int)(np < lag_planes ? np : lag_planes);
   const long long nitems = np * 2LL * ITEMS;
   long long ahead = 0;  // thread 0: the next item's index, claimed at this item's start
+  const uint32_t spin = dep_wait_limit(status, kXyL2Spin);
   if (threadIdx.x == 0) {
     mbar_init(bar, 1);
     mbar_fence_init();
@@ -275,7 +276,7 @@ __global__ void __launch_bounds__(kXyL2Threads, 8) k_xy_l2(const __grid_constant
     const int slot = (int)(p % ring);
     if (threadIdx.x == 0) {
       if (is_y) {
-        if (!wait_count(xdone + p, ITEMS)) ok = false;
+        if (!wait_count(xdone + p, ITEMS, spin)) ok = false;
         asm volatile("fence.proxy.async.global;" ::: "memory");  // generic stores -> TMA reads
         mbar_arrive_expect_tx(bar, (uint32_t)(C * N * 8));
         Cfg::load_y(smem_u32(tile), &mscr, tl * C, slot, bar);
@@ -335,7 +336,7 @@ __global__ void __launch_bounds__(kXyL2Threads, 8) k_xy_l2(const __grid_constant
     } else {
       const int t = threadIdx.x % T, c = threadIdx.x / T;
       if (p >= ring) {  // the slot's previous plane must have been read
-        if (threadIdx.x == 0 && !wait_count(yread + (p - ring), ITEMS)) ok = false;
+        if (threadIdx.x == 0 && !wait_count(yread + (p - ring), ITEMS, spin)) ok = false;
         __syncthreads();
       }
       float2 *o = scratch + (long long)slot * N * N + (long long)(tl * C + c) * N + t;

@@ -70,7 +70,9 @@ int convgpu_conv3d_device(unsigned N, const float2 *d_sig, const float2 *d_filte
  * CONVGPU_EINVAL. CONVGPU_TENSOR_SPLIT returns CONVGPU_EUNSUPPORTED.
  * The first call on a device sets that device up (looks up the array's address and
  * fills a twiddle table), so make it before any stream capture. All calls share the
- * array: calls that overlap on the GPU race. */
+ * array: calls that overlap on the GPU race. Like convgpu_conv3d_device it returns once
+ * the work is enqueued; a kernel that gives up a bounded wait reports it through
+ * convgpu_device_status, not through this call's return code. */
 #define CONVGPU_NOALLOC_SCRATCH_ELEMS (1u << 21)
 int convgpu_conv3d_device_noalloc(unsigned N, const float2 *d_sig, const float2 *d_filter, float2 *d_out,
                                   unsigned how_many, unsigned flags, void *stream);
@@ -173,6 +175,27 @@ int convgpu_plan_variant(unsigned N, int kind, int set_to);
  * their own kernels, read and clear the word themselves and then return an fpga_t with
  * valid == 0; stream-ordered device calls leave it for this function. */
 int convgpu_device_status(unsigned *status);
+
+/* Testing hooks for the failure contract (no counterpart in pc2/ConvFPGA, whose runtime
+ * errors exit() the process: host/src/opencl_utils.c:421-439). Neither is meant for
+ * production use; both leave every result path intact.
+ *
+ * convgpu_debug_dependency_wait_limit: every bounded wait of a kernel on a counter that
+ * other CTAs advance (plane dependencies of the fused x+y pass, the uneven work queue, the
+ * grid barriers of the one-launch small-cube path) gives up after `probes` probes
+ * (0: at once); probes < 0 restores each wait's own limit. A wait that gives up sets its
+ * status bit (2 or 16 above) and the kernel finishes without waiting, so the output is
+ * wrong and the call reports it: host-buffer calls return valid == 0, device calls leave
+ * the bit for convgpu_device_status. Waits for copies or MMAs in flight are not affected.
+ * Waits for the device before it changes the limit; graphs captured earlier read the new
+ * limit when they run.
+ *
+ * convgpu_debug_fail_allocations: the next `count` allocations of the library's
+ * grow-only device buffers (workspace, host-pipeline staging) fail as out of memory; the
+ * call that meets one returns CONVGPU_ENOMEM or an fpga_t with valid == 0, and later
+ * calls allocate again. */
+int convgpu_debug_dependency_wait_limit(int probes);
+int convgpu_debug_fail_allocations(unsigned count);
 
 /* Text of the calling thread's last error ("" if none). */
 const char *convgpu_last_error(void);

@@ -103,3 +103,25 @@ def test_flag_and_code_constants_match_the_header():
                  "UNEVEN_PER_JOB", "UNEVEN_QUEUE", "HOST_SLABS", "FILTER_CACHED", "FILTER_REAL"):
         assert flag in defs and hasattr(cg, flag), flag
     assert checked >= 10
+
+
+def test_uneven_batch_rejects_malformed_jobs_without_a_gpu(built_lib):
+    """Descriptors are checked before anything runs (the base addresses below are never
+    dereferenced): unsupported sizes, offsets past the address space, outputs that overlap
+    another job's output or part of the job's own signal."""
+    base = 1 << 20
+
+    def call(jobs, same_io=False):
+        arr = (cg.Job * len(jobs))(*[cg.Job(*j) for j in jobs])
+        out = base if same_io else base + (1 << 30)
+        return built_lib.convgpu_conv3d_uneven_device(arr, len(jobs), base, base + (1 << 29), out, 0, None)
+
+    v = 32 ** 3
+    assert call([(48, 0, 0, 0)]) == cg.EINVAL
+    assert "size 48" in cg.last_error()
+    assert call([(32, 0, 0, 1 << 62)]) == cg.EINVAL                  # byte offset wraps
+    assert "address space" in cg.last_error()
+    assert call([(32, 0, 0, 0), (32, v, v, v - 1)]) == cg.EINVAL     # outputs overlap by one value
+    assert "overlap" in cg.last_error()
+    assert call([(32, 0, 0, 10)], same_io=True) == cg.EINVAL         # shifted in-place output
+    assert "own signal" in cg.last_error()
