@@ -631,7 +631,7 @@ def run_configs(a) -> None:
     """The other single-GPU workloads, timed on device buffers (K steps after W warm-up
     steps, CUDA events): 64^3 x1 (signal and filter U[-1,1], normalised), 128^3 x8 (shared
     real periodic Gaussian filter, sigma 4) and 512^3 x1 (shared real periodic Gaussian
-    filter, sigma 6). The real filters are passed as floats (CONVGPU_FILTER_REAL). Inputs
+    filter, sigma 6), the last on both the FP32 and the tensor-core split path. The real filters are passed as floats (CONVGPU_FILTER_REAL). Inputs
     are generated on the device with the workloads' shapes; for timing, the 512^3 signal is
     U[-1,1] noise instead of the workload's sum of Gaussian blobs."""
     import torch
@@ -659,13 +659,16 @@ def run_configs(a) -> None:
         return torch.exp(-r2 / (2.0 * sigma * sigma)).contiguous()
 
     results = {}
-    for name, n, b in (("c64x1", 64, 1), ("c128x8", 128, 8), ("c512x1", 512, 1)):
-        cg.autotune([n], write_cache=False)
+    for name, n, b in (("c64x1", 64, 1), ("c128x8", 128, 8), ("c512x1", 512, 1), ("c512x1_tc", 512, 1)):
+        if name != "c512x1_tc":
+            cg.autotune([n], write_cache=False)
         sig = uni((b, n, n, n))
         if name == "c64x1":
             filt, flags = uni((n, n, n)), cg.NORMALIZE
         else:
             filt, flags = gauss(n, 4.0 if n == 128 else 6.0), cg.FILTER_REAL | cg.NORMALIZE
+        if name == "c512x1_tc":
+            flags |= cg.TENSOR_SPLIT  # the tcgen05 split-TF32 kernels of N = 512
         out = torch.empty_like(sig)
         steps = max(3, a.steps if n < 512 else min(a.steps, 20))
         for _ in range(a.warmup):
@@ -682,7 +685,8 @@ def run_configs(a) -> None:
         model = (48 + 88 * b) * n ** 3  # one shared filter + b signals, per-axis pass model
         results[name] = {"conv_per_s": round(b / (ms / 1e3), 1), "ms_per_step": round(ms, 4),
                          "model_gbs": round(model / (ms / 1e3) / 1e9, 1), "steps": steps,
-                         "filter": "complex U[-1,1]" if name == "c64x1" else "real Gaussian (FILTER_REAL)"}
+                         "filter": "complex U[-1,1]" if name == "c64x1" else "real Gaussian (FILTER_REAL)",
+                         "path": "tcgen05 split-TF32" if flags & cg.TENSOR_SPLIT else "plain FP32"}
         del sig, filt, out
         torch.cuda.empty_cache()
     status = cg.device_status()

@@ -323,10 +323,14 @@ static cudaError_t pass_xy(int n, const float2 *src, float2 *dst, int nvol, bool
   return e;
 }
 
-// The tensor-core path has its own x and y kernels for N = 256 only; at other sizes it runs
-// the FP32 kernels, the fused pass included, so its results equal the FP32 path's.
+// True when the tensor-core path has kernels of its own for size n (N = 256; N = 512 in
+// TF32x3); elsewhere it runs the FP32 kernels, the fused x+y pass included, and its
+// results equal the FP32 path's.
+static bool tc_kernels(int n, int tc) {
+  return tc != 0 && (n == 256 || (n == 512 && tc - 1 == kTcTf32x3));
+}
 static bool use_xy(int n, int tc) {
-  return (tc == 0 || n != 256) && (n == 128 || n == 256 || n == 512) && get_pass_variant(n, kKindXy) != 0;
+  return !tc_kernels(n, tc) && (n == 128 || n == 256 || n == 512) && get_pass_variant(n, kKindXy) != 0;
 }
 
 // ------------------------------------------------------------------ pass sequences

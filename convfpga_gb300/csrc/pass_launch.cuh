@@ -248,6 +248,8 @@ namespace convgpu {
 // Tensor-core pass for N = 256 (passes_n256.cu); bf16x3 selects BF16x3 over TF32x3.
 cudaError_t launch_tc256_entry(const PassReq &r, int bf16x3);
 cudaError_t launch_tc05_entry(const PassReq &r);
+// tcgen05 split-TF32 pass for N = 512 (tc05_n512.cu).
+cudaError_t launch_tc05_512_entry(const PassReq &r);
 // L2-staged fused x + y pass for N = 128, 256 or 512 (xyl2.cu, xyl2.cuh).
 cudaError_t launch_xy_l2(int n, const float2 *src, float2 *dst, int nplanes, bool inverse, float scale,
                          const float2 *tw512, unsigned *status, cudaStream_t s);

@@ -308,9 +308,12 @@ cudaError_t launch_axis_pass_real(int n, const float *src, float2 *dst, int nvol
 cudaError_t launch_axis_pass_tc(int n, int axis, int op, const float2 *src, float2 *dst, const float2 *filt,
                                 long long filt_vol_elems, int nvol, float scale, const float2 *tw512,
                                 cudaStream_t s, int prec) {
-  // The tensor-core kernels cover N = 256 (two radix-16 stages per axis); other sizes,
-  // and operands that tensor maps cannot describe, run the FP32 kernels.
-  if (n != 256 || nvol <= 0 || !g_use_tma)
+  // The tensor-core kernels cover N = 256 (two radix-16 stages per axis, TF32x3 on tcgen05
+  // or mma.sync, BF16x3 on mma.sync) and N = 512 in TF32x3 (a radix-2 step around two
+  // 256-point tcgen05 transforms); other sizes and precisions, and operands that tensor
+  // maps cannot describe, run the FP32 kernels.
+  const bool tc512 = n == 512 && prec == kTcTf32x3;
+  if ((n != 256 && !tc512) || nvol <= 0 || !g_use_tma)
     return launch_axis_pass(n, axis, op, src, dst, filt, filt_vol_elems, nvol, scale, tw512, s);
   if ((op == OP_CONV || op == OP_CONV_FZ) && axis != 2) return cudaErrorInvalidValue;
   PassReq r{};
@@ -323,7 +326,8 @@ cudaError_t launch_axis_pass_tc(int n, int axis, int op, const float2 *src, floa
   r.s = s;
   // split TF32: tcgen05 kernels (plan kind kKindTc, variant 0) or mma.sync (variant 1);
   // BF16x3: mma.sync
-  const cudaError_t e = (prec == kTcTf32x3 && get_pass_variant(n, kKindTc) == 0)
+  const cudaError_t e = tc512 ? launch_tc05_512_entry(r)
+                        : (prec == kTcTf32x3 && get_pass_variant(n, kKindTc) == 0)
                             ? launch_tc05_entry(r)
                             : launch_tc256_entry(r, prec == kTcBf16x3 ? 1 : 0);
   if (e == cudaErrorNotSupported)

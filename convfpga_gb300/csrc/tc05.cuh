@@ -1,6 +1,7 @@
-// Tensor-core split-precision passes for N = 256 on the 5th-generation tensor cores
-// (tcgen05): operands from shared-memory matrix descriptors, accumulators in tensor
-// memory (TMEM), one thread issuing the MMAs, completion tracked on an mbarrier.
+// Tensor-core split-precision passes for N = 256 and 512 on the 5th-generation tensor
+// cores (tcgen05): operands from shared-memory matrix descriptors, accumulators in tensor
+// memory (TMEM), one thread issuing the MMAs, completion tracked on an mbarrier. (N = 512:
+// a radix-2 step around two 256-point transforms, k_tc05_512 at the end of this file.)
 //
 // A 256-point transform is 16 x 16 (four-step). A CTA holds P pencils (P = 8 or 16),
 // i.e. 16 P instances of each 16-point stage; thread m owns instance m and its A row
@@ -100,7 +101,7 @@ __device__ __forceinline__ void t5_fence_after() { asm volatile("tcgen05.fence::
 // One-block kernel writing the constant block: B[o][k] with o = output (re k2, then im
 // k2), k = input (re n2, then im n2); W16^(k2 n2) = (c, -s) gives re = xr c + xi s,
 // im = -xr s + xi c. Split into TF32 hi and lo parts in the swizzled layout.
-__global__ void k_tc05_consts(unsigned char *blk, const float2 *tw512) {
+static __global__ void k_tc05_consts(unsigned char *blk, const float2 *tw512) {
   for (int i = threadIdx.x; i < 32 * 32; i += blockDim.x) {
     const int o = i >> 5, k = i & 31;
     const float2 w = tw512[32 * (((o & 15) * (k & 15)) & 15)];
@@ -410,6 +411,201 @@ __global__ void __launch_bounds__(T5Geom<P>::kThreads, T5Geom<P>::kMinBlocks)
       if (a.scale != 1.0f) v = make_float2(v.x * a.scale, v.y * a.scale);
       dst[(long long)(ia + 16 * k1) * a.axis_stride] = v;
     }
+  }
+}
+
+// ------------------------------------------------------------------ N = 512
+// A 512-point transform is one radix-2 step on the CUDA cores around two 256-point
+// transforms on the tensor cores (t5_fft256 with P = 8 sub-pencils):
+//   forward, decimation in frequency: u[p] = x[p] + x[p+256], w[p] = (x[p] - x[p+256]) W512^p
+//     for p < 256; X[2k] = DFT256(u)[k], X[2k+1] = DFT256(w)[k];
+//   inverse, decimation in time: E = IDFT256(X[2m]), O = IDFT256(X[2m+1]);
+//     x[n] = E[n] + W512^-n O[n], x[n+256] = E[n] - W512^-n O[n] for n < 256.
+// A CTA holds 4 pencils of 512 (4 columns of a y / z tile, or 4 rows of an x tile), i.e. 8
+// sub-pencils of 256, so every tensor-core stage is one M = 128 tile, as for N = 256 with 8
+// pencils. Sub-pencil j of pencil c (j = 0: u / even outputs, 1: w / odd outputs) is
+// sub-column b = 4j + c of the strided mapping (thread m = 8a + b) or sub-row a = 2c + j
+// of the row mapping (thread m = 16a + b); the threads that combine E and O are lanes m and
+// m ^ 4 (strided) or m ^ 16 (rows) of one warp and exchange through a shuffle. The forward
+// transform leaves X[2(q + 16k) + j] in the registers of thread (q, j, c); the fused z ops
+// multiply both operands in that order and start the inverse from it, the plain forward
+// pass stores it to positions 2(q + 16k) + j. Twiddles W512^p come from the engine's FP32
+// table (generated in FP64), read through L1.
+template <int OP, bool ROWS>
+__global__ void __launch_bounds__(T5Geom<8>::kThreads, T5Geom<8>::kMinBlocks)
+    k_tc05_512(const __grid_constant__ CUtensorMap msrc, const __grid_constant__ CUtensorMap mfilt, PassArgs a,
+               int axis) {
+  using G = T5Geom<8>;
+  constexpr int N = 512, P = 4, TILE = N * P;  // 4 pencils: 16 KB, one A part
+  static_assert(TILE * 8 == G::kABytes, "a tile is one A operand part");
+  constexpr bool HAS_F = (OP == OP_CONV || OP == OP_CONV_FZ);
+  constexpr uint32_t kCols = HAS_F ? 64u : 32u;
+  static_assert(!(ROWS && HAS_F), "fused ops are z passes");
+  extern __shared__ __align__(1024) unsigned char smraw[];
+  if (smem_u32(smraw) & 1023u) {
+    if (threadIdx.x == 0 && a.status) atomicOr(a.status, kStatusSmemAlign);
+    return;
+  }
+  float2 *tile = reinterpret_cast<float2 *>(smraw);
+  float2 *ftile = reinterpret_cast<float2 *>(smraw + G::kABytes);
+  const float2 *tw = reinterpret_cast<const float2 *>(smraw + G::kOffTw);
+  const uint32_t tbar = smem_u32(smraw + G::kOffBar), mbar = tbar + 8;
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(smraw + G::kOffBar + 16);
+
+  int vol = 0, row = 0, x0 = 0;
+  long long row0 = 0;
+  if (ROWS) {
+    row0 = (long long)blockIdx.x * P;
+  } else {
+    vol = blockIdx.x / a.groups_per_vol;
+    const int rr = blockIdx.x % a.groups_per_vol;
+    row = rr / a.groups_x;
+    x0 = (rr % a.groups_x) * P;
+  }
+  if (threadIdx.x == 0) {
+    mbar_init(tbar, 1);
+    mbar_init(mbar, 1);
+    mbar_fence_init();
+    mbar_arrive_expect_tx(tbar, (HAS_F ? 2u : 1u) * TILE * 8u + (uint32_t)kT5ConstBytes);
+    if (ROWS) {
+      tma_load_3d(smem_u32(tile), &msrc, 0, 0, (int)row0, tbar);  // rows viewed as (256, 2, rows)
+    } else {
+#pragma unroll
+      for (int l = 0; l < 2; ++l) {  // a box is at most 256 long
+        if (axis == 1)
+          tma_load_3d(smem_u32(tile + l * 256 * P), &msrc, x0, 256 * l, vol * N + row, tbar);
+        else
+          tma_load_3d(smem_u32(tile + l * 256 * P), &msrc, x0, row, vol * N + 256 * l, tbar);
+        if constexpr (HAS_F)
+          tma_load_3d(smem_u32(ftile + l * 256 * P), &mfilt, x0, row, (a.filt_vol_elems ? vol : 0) * N + 256 * l,
+                      tbar);
+      }
+    }
+    bulk_load(smem_u32(smraw + G::kOffB), reinterpret_cast<const unsigned char *>(a.tw512) + kT5ConstOffset,
+              (uint32_t)kT5ConstBytes, tbar);
+  }
+  if (threadIdx.x < 32) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)),
+                 "n"(kCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  t5_fence_before();
+  __syncthreads();
+  t5_fence_after();
+  T5Ctx<8> cx;
+  cx.ah = smraw;
+  cx.al = smraw + G::kABytes;
+  cx.bh = smem_u32(smraw + G::kOffB);
+  cx.bl = cx.bh + kT5BBytes;
+  cx.tmem = *tslot;
+  cx.bar = mbar;
+  cx.phase = 0;
+  cx.ok = 1;
+
+  const int loaded = __syncthreads_and(mbar_wait_bounded(tbar, 0) ? 1 : 0);
+  if (!loaded) {
+    if (threadIdx.x == 0 && a.status) atomicOr(a.status, kStatusTmaTimeout);
+    mbar_wait_bounded(tbar, 0);
+    t5_fence_before();
+    __syncthreads();
+    t5_fence_after();
+    if (threadIdx.x < 32) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(cx.tmem), "n"(kCols));
+    return;
+  }
+
+  const int m = threadIdx.x;
+  const int ia = ROWS ? (m >> 4) : (m >> 3), ib = ROWS ? (m & 15) : (m & 7);
+  const int j = ROWS ? (ia & 1) : (ib >> 2);   // sub-pencil: even (0) or odd (1) outputs
+  const int c = ROWS ? (ia >> 1) : (ib & 3);   // pencil of the tile
+  const int q = ROWS ? ib : ia;                // this thread's 256-positions are q + 16 i
+  const int partner = ROWS ? 16 : 4;           // lane of the other sub-pencil of the pencil
+  const float sgn = j ? -1.f : 1.f;
+  auto at = [&](const float2 *t, int p) -> float2 { return ROWS ? t[c * N + p] : t[p * P + c]; };
+  // forward: stage-1 inputs of sub-pencil j, u or w at positions q + 16 n2 (the product
+  // with (1, 0) for j = 0 is exact, so both sub-pencils take one branch-free path)
+  auto gather_dif = [&](const float2 *t, float2 (&x)[16]) {
+#pragma unroll
+    for (int n2 = 0; n2 < 16; ++n2) {
+      const int p = q + 16 * n2;
+      const float2 u = at(t, p), v = at(t, p + 256);
+      const float2 d = make_float2(fmaf(sgn, v.x, u.x), fmaf(sgn, v.y, u.y));
+      x[n2] = cmul(d, j ? __ldg(a.tw512 + p) : make_float2(1.f, 0.f));
+    }
+  };
+  // inverse: stage-1 inputs of sub-pencil j from a natural-order spectrum, X[2(q + 16 n2) + j]
+  auto gather_dit = [&](const float2 *t, float2 (&x)[16]) {
+#pragma unroll
+    for (int n2 = 0; n2 < 16; ++n2) x[n2] = at(t, 2 * (q + 16 * n2) + j);
+  };
+  // after IDFT256 of both sub-pencils: x holds E (j = 0) or O (j = 1) at n = q + 16 k;
+  // returns x[n] (j = 0) or x[n + 256] (j = 1)
+  auto combine = [&](float2 (&x)[16]) {
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+      const float2 w = __ldg(a.tw512 + q + 16 * k);
+      const float2 t = cmul(x[k], j ? make_float2(w.x, -w.y) : make_float2(1.f, 0.f));
+      const float rx = __shfl_xor_sync(0xffffffffu, t.x, partner);
+      const float ry = __shfl_xor_sync(0xffffffffu, t.y, partner);
+      x[k] = make_float2(fmaf(sgn, t.x, rx), fmaf(sgn, t.y, ry));
+    }
+  };
+
+  float2 x[16];
+  bool natural = true;  // outputs at n = q + 16 k + 256 j, else at 2(q + 16 k) + j
+  if constexpr (OP == OP_FWD) {
+    gather_dif(tile, x);
+    __syncthreads();  // tile consumed before A (which aliases it) is written
+    t5_fft256<8, ROWS>(cx, x, tw);
+    natural = false;
+  } else if constexpr (OP == OP_INV) {
+    gather_dit(tile, x);
+#pragma unroll
+    for (int k = 0; k < 16; ++k) x[k] = cswap(x[k]);
+    __syncthreads();
+    t5_fft256<8, ROWS>(cx, x, tw);
+#pragma unroll
+    for (int k = 0; k < 16; ++k) x[k] = cswap(x[k]);
+    combine(x);
+  } else {
+    float2 f[16];
+    if constexpr (OP == OP_CONV_FZ) {
+      gather_dif(tile, x);
+      t5_stash_st<8>(cx, x);  // signal parked while the filter is transformed
+      gather_dif(ftile, f);
+      __syncthreads();
+      t5_fft256<8, false>(cx, f, tw);
+      t5_stash_ld<8>(cx, x);
+      t5_stash_st<8>(cx, f);
+    } else {
+      gather_dit(ftile, f);  // the spectrum in the forward transform's register order
+      t5_stash_st<8>(cx, f);
+      gather_dif(tile, x);
+      __syncthreads();
+    }
+    t5_fft256<8, false>(cx, x, tw);
+    t5_stash_ld<8>(cx, f);
+#pragma unroll
+    for (int k = 0; k < 16; ++k) x[k] = cswap(cmul(x[k], f[k]));
+    t5_fft256<8, false>(cx, x, tw);
+#pragma unroll
+    for (int k = 0; k < 16; ++k) x[k] = cswap(x[k]);
+    combine(x);
+  }
+  t5_fence_before();
+  __syncthreads();
+  t5_fence_after();
+  if (threadIdx.x < 32) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(cx.tmem), "n"(kCols));
+  if (!cx.ok && threadIdx.x == 0 && a.status) atomicOr(a.status, kStatusMmaTimeout);
+
+  float2 *dst = ROWS ? a.dst + (row0 + c) * N
+                     : a.dst + (long long)vol * a.vol_elems + (long long)row * a.plane_pitch + x0 + c;
+  const long long es = ROWS ? 1 : a.axis_stride;
+#pragma unroll
+  for (int k = 0; k < 16; ++k) {
+    float2 v = x[k];
+    if (a.scale != 1.0f) v = make_float2(v.x * a.scale, v.y * a.scale);
+    const int pos = natural ? q + 16 * k + 256 * j : 2 * (q + 16 * k) + j;
+    dst[(long long)pos * es] = v;
   }
 }
 

@@ -4,9 +4,8 @@ The oracle is the same pipeline in complex128 (pocketfft). Each case prints one 
 workload, path, relative L2 error, max-abs error, and max |reference|.
   - FP32 path: rel-L2 < 1e-6 (the reference's 120 dB criterion, src/fft_conv3D.cpp:236-258)
     and max-abs < 1e-5 * max |reference|.
-  - Tensor-core split path (CONVGPU_TENSOR_SPLIT, TF32x3): rel-L2 <= 1e-5. Only N = 256 has
-    tensor-core kernels; at 512^3 the flag runs the FP32 kernels, so the two results are
-    asserted to be identical.
+  - Tensor-core split path (CONVGPU_TENSOR_SPLIT, TF32x3): rel-L2 <= 1e-5 at 256^3 and 512^3,
+    both of which have tensor-core kernels (the result differs from the FP32 path's).
 Inputs are the workloads' seeded synthetic cubes (oracle.make_config), with the
 workloads' options: 64^3 normalised by 1/N^3, shared real Gaussian filters passed as real
 (CONVGPU_FILTER_REAL), per-signal filters at 256^3, one filter per job in the uneven batch.
@@ -58,8 +57,7 @@ def test_uniform_workloads_against_fp64(gpu, name):
         tc = _device(gpu, sig, filt, flags | gpu.TENSOR_SPLIT, real)
         e_tc, _, _ = _report(name, "tf32x3", ref, tc)
         assert e_tc <= REL_TC
-        if name == "c512x1":
-            np.testing.assert_array_equal(tc, out)
+        assert not np.array_equal(tc, out)  # the tensor-core kernels ran
     assert gpu.device_status() == 0
 
 

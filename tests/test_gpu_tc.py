@@ -1,8 +1,9 @@
 """Tensor-core split-precision path (CONVGPU_TENSOR_SPLIT) through the C ABI.
 
 Radix-16 stages of the N = 256 transforms run as split-precision complex matmuls with
-FP32 accumulation (default TF32x3; BF16x3 on request); sizes without a tensor-core kernel
-run the FP32 kernels. Split TF32 has two kernel families (plan kind 5): tcgen05 with
+FP32 accumulation (default TF32x3; BF16x3 on request); N = 512 in TF32x3 runs one radix-2
+step on the CUDA cores around two such 256-point transforms; sizes without a tensor-core
+kernel run the FP32 kernels. Split TF32 has two kernel families (plan kind 5): tcgen05 with
 TMEM accumulators (variant 0, default) and mma.sync (variant 1); both are checked. Tolerance: the relative-L2 error against the FP64 oracle stays at
 or below 1e-5 (the workload's stated bound for this path); the max-abs error is reported
 beside it. BF16x3 is held to 3e-5: it measures about 1.4e-5 on the 256^3 workload and
@@ -134,6 +135,62 @@ def test_tc_host_entry_point(gpu):
     assert t.valid, gpu.last_error()
     ref = conv3d(sig, filt, "fp64", engine="pocketfft")
     assert rel_l2(ref, out) <= REL_L2_TC
+
+
+def _dev(cg, s, f, b, flags):
+    o = torch.empty_like(s)
+    cg.conv3d_device(s.shape[-1], s, f, o, b, flags)
+    torch.cuda.synchronize()
+    return o
+
+
+def _rel_dev(ref, out):
+    """Relative L2 error of two device tensors, computed on the device (no FFT involved)."""
+    return float(torch.linalg.vector_norm(out - ref) / torch.linalg.vector_norm(ref))
+
+
+@pytest.mark.slow
+@pytest.mark.parametrize("route", ["per_signal_fz", "shared3_conv", "spectrum_conv"])
+def test_tc_512_routes_against_fp32(gpu, route):
+    """Every pass of the 512^3 tensor-core path (x, y, fused z with and without the filter's
+    z transform, the filter's own z pass, inverses) against the FP32 path on the same inputs,
+    which is itself within 1e-6 of FP64 (test_gpu_config_errors): the TF32x3 error stays at
+    or below 1e-5, and it is not zero (the tensor-core kernels ran)."""
+    n = 512
+    g = torch.Generator(device="cuda").manual_seed(512)
+    b = 3 if route == "shared3_conv" else 1
+    s = torch.complex(torch.randn((b, n, n, n), device="cuda", generator=g),
+                      torch.randn((b, n, n, n), device="cuda", generator=g))
+    fshape = (b, n, n, n) if route == "per_signal_fz" else (n, n, n)
+    f = torch.complex(torch.rand(fshape, device="cuda", generator=g) * 2 - 1,
+                      torch.rand(fshape, device="cuda", generator=g) * 2 - 1)
+    flags = {"per_signal_fz": gpu.FILTER_PER_SIGNAL, "shared3_conv": 0, "spectrum_conv": gpu.FILTER_IS_SPECTRUM}[route]
+    if route == "spectrum_conv":
+        spec = torch.empty_like(f)
+        gpu.filter_spectrum_device(n, f, spec, 1)
+        f = spec
+    fp32 = _dev(gpu, s, f, b, flags)
+    tc = _dev(gpu, s, f, b, flags | gpu.TENSOR_SPLIT)
+    err = _rel_dev(fp32, tc)
+    print(f"512^3 {route}: TC vs FP32 rel-L2 {err:.3e}")
+    assert 0.0 < err <= REL_L2_TC
+    assert gpu.device_status() == 0
+
+
+@pytest.mark.slow
+def test_tc_512_impulse_reproduces_filter(gpu):
+    """A shifted unit impulse gives the filter rolled by the shift: every position mapping
+    of the 512-point tensor-core passes (the even / odd sub-transforms and their combine)."""
+    n = 512
+    shift = (5, 509, 300)
+    s = torch.zeros((1, n, n, n), dtype=torch.complex64, device="cuda")
+    s[0][shift] = 1.0
+    g = torch.Generator(device="cuda").manual_seed(513)
+    f = torch.complex(torch.rand((n, n, n), device="cuda", generator=g) * 2 - 1,
+                      torch.rand((n, n, n), device="cuda", generator=g) * 2 - 1)
+    out = _dev(gpu, s, f, 1, gpu.TENSOR_SPLIT | gpu.NORMALIZE)
+    ref = torch.roll(f, shifts=shift, dims=(0, 1, 2))[None]
+    assert _rel_dev(ref, out) <= REL_L2_TC
 
 
 def test_tc_device_status_clean(gpu):
