@@ -295,12 +295,12 @@ static cudaError_t pass(int n, int axis, int op, const float2 *src, float2 *dst,
   return e;
 }
 
-// Fused x + y pass (plan kind kKindXy: 1 L2-staged (N = 128, 256, 512), 2 8-CTA clusters
-// (N = 256)). Returns
-// cudaErrorNotSupported when it cannot run, in which case the caller runs the x and y
-// passes separately.
+// Fused x + y pass: for the FP32 path plan kind kKindXy (1 L2-staged (N = 128, 256, 512),
+// 2 8-CTA clusters (N = 256)); for the tensor-core path (tc != 0) the L2-staged pass on
+// tcgen05 (N = 256). Returns cudaErrorNotSupported when it cannot run, in which case the
+// caller runs the x and y passes separately.
 static cudaError_t pass_xy(int n, const float2 *src, float2 *dst, int nvol, bool inverse, float scale,
-                           cudaStream_t s) {
+                           cudaStream_t s, int tc = 0) {
   PassRec r{12 + (inverse ? 1 : 0), 0.0, nullptr, nullptr};
   if (g_prof) {
     r.bytes = 4.0 * (double)n * n * n * 8.0 * nvol;  // the x and y passes it replaces
@@ -308,7 +308,8 @@ static cudaError_t pass_xy(int n, const float2 *src, float2 *dst, int nvol, bool
     cudaEventCreate(&r.b);
     cudaEventRecord(r.a, s);
   }
-  cudaError_t e = launch_xy_pass(n, src, dst, nvol * n, inverse, scale, g.tw512, s, get_pass_variant(n, kKindXy));
+  cudaError_t e = tc ? launch_xy_l2_tc_pass(src, dst, nvol * n, inverse, scale, g.tw512, s)
+                     : launch_xy_pass(n, src, dst, nvol * n, inverse, scale, g.tw512, s, get_pass_variant(n, kKindXy));
   if (g_prof) {
     cudaEventRecord(r.b, s);
     if (e == cudaSuccess) {
@@ -319,7 +320,7 @@ static cudaError_t pass_xy(int n, const float2 *src, float2 *dst, int nvol, bool
     }
   }
   // the L2-staged pass is two launches: counter clear + pass
-  if (e == cudaSuccess) count_launches(get_pass_variant(n, kKindXy) == 1 ? 2 : 1);
+  if (e == cudaSuccess) count_launches((tc || get_pass_variant(n, kKindXy) == 1) ? 2 : 1);
   return e;
 }
 
@@ -330,7 +331,10 @@ static bool tc_kernels(int n, int tc) {
   return tc != 0 && (n == 256 || (n == 512 && tc - 1 == kTcTf32x3));
 }
 static bool use_xy(int n, int tc) {
-  return !tc_kernels(n, tc) && (n == 128 || n == 256 || n == 512) && get_pass_variant(n, kKindXy) != 0;
+  if (tc_kernels(n, tc))  // the tcgen05 split-TF32 kernels of N = 256 have a fused form
+    return n == 256 && tc - 1 == kTcTf32x3 && get_pass_variant(256, kKindTc) == 0 &&
+           get_pass_variant(256, kKindTcXy) == 1;
+  return (n == 128 || n == 256 || n == 512) && get_pass_variant(n, kKindXy) != 0;
 }
 
 // ------------------------------------------------------------------ pass sequences
@@ -363,7 +367,8 @@ static cudaError_t pass_real(int n, const float *filt, float2 *spec, int count, 
 // `real`, filt holds N^3 floats per filter (CONVGPU_FILTER_REAL); spec must not overlap it.
 static cudaError_t enqueue_filter(int n, const float2 *filt, float2 *spec, int count, bool xy_only,
                                   cudaStream_t s, int tc = 0, bool real = false) {
-  cudaError_t xe = (!real && use_xy(n, tc)) ? pass_xy(n, filt, spec, count, false, 1.f, s) : cudaErrorNotSupported;
+  cudaError_t xe =
+      (!real && use_xy(n, tc)) ? pass_xy(n, filt, spec, count, false, 1.f, s, tc) : cudaErrorNotSupported;
   if (xe != cudaSuccess && xe != cudaErrorNotSupported) return xe;
   if (xe == cudaErrorNotSupported) {
     if (real)
@@ -381,7 +386,7 @@ static cudaError_t enqueue_filter(int n, const float2 *filt, float2 *spec, int c
 static cudaError_t enqueue_signals(int n, const float2 *sig, float2 *out, const float2 *spec,
                                    long long spec_vol, int fop, int nsig, float scale, cudaStream_t s,
                                    cudaEvent_t mid, int tc = 0) {
-  cudaError_t xe = use_xy(n, tc) ? pass_xy(n, sig, out, nsig, false, 1.f, s) : cudaErrorNotSupported;
+  cudaError_t xe = use_xy(n, tc) ? pass_xy(n, sig, out, nsig, false, 1.f, s, tc) : cudaErrorNotSupported;
   if (xe != cudaSuccess && xe != cudaErrorNotSupported) return xe;
   const bool fused = xe == cudaSuccess;
   if (!fused) {
@@ -391,7 +396,7 @@ static cudaError_t enqueue_signals(int n, const float2 *sig, float2 *out, const 
   CG_TRY(pass(n, 2, fop, out, out, spec, spec_vol, nsig, 1.f, s, tc));
   if (mid) cudaEventRecord(mid, s);
   if (fused) {
-    const cudaError_t e = pass_xy(n, out, out, nsig, true, scale, s);
+    const cudaError_t e = pass_xy(n, out, out, nsig, true, scale, s, tc);
     if (e == cudaSuccess) return cudaSuccess;
     if (e != cudaErrorNotSupported) return e;
   }
@@ -987,7 +992,7 @@ Timing bridge_conv_host(unsigned n, const void *sig, const void *filt, void *out
 // (src/fft_conv3D.cpp:85-112): one line per cube size with the shape variant chosen for
 // each pass kind and the timings (microseconds per launch, variants 0 and 1) it was
 // chosen from.
-static const char *kKindNames[kPassKinds] = {"rows", "strided", "conv", "conv_fz", "xy", "tc"};
+static const char *kKindNames[kPassKinds] = {"rows", "strided", "conv", "conv_fz", "xy", "tc", "tcxy"};
 
 static void load_plan_cache(const std::string &path) {
   FILE *f = std::fopen(path.c_str(), "r");
@@ -1089,6 +1094,42 @@ int bridge_autotune(const unsigned *sizes, unsigned count, int write_cache) {
             count_launches(14);
           } else if (err == cudaErrorNotSupported) {
             err = cudaSuccess;
+          }
+        }
+        row.choice[k] = row.us[1][k] < row.us[0][k] ? 1 : 0;
+        set_pass_variant(n, k, row.choice[k]);
+        continue;
+      }
+      if (k == kKindTcXy) {
+        // x and y passes of the split-TF32 path (tcgen05, N = 256): separate passes
+        // (variant 0) against the L2-staged fused pass (variant 1)
+        for (int v = 0; v < 2; ++v) row.us[v][k] = 0.0;
+        if (n == 256) {
+          for (int v = 0; v < 2 && err == cudaSuccess; ++v) {
+            auto run = [&]() {
+              if (v == 1) return launch_xy_l2_tc_pass(data, data, nvol * n, false, 1.f, g.tw512, s);
+              cudaError_t r = launch_axis_pass_tc(n, 0, OP_FWD, data, data, nullptr, 0, nvol, 1.f, g.tw512, s,
+                                                  kTcTf32x3);
+              if (r == cudaSuccess)
+                r = launch_axis_pass_tc(n, 1, OP_FWD, data, data, nullptr, 0, nvol, 1.f, g.tw512, s, kTcTf32x3);
+              return r;
+            };
+            const int keep = get_pass_variant(n, kKindTc);
+            set_pass_variant(n, kKindTc, 0);
+            for (int w = 0; w < 2 && err == cudaSuccess; ++w) err = run();
+            cudaEventRecord(e0, s);
+            for (int t = 0; t < 5 && err == cudaSuccess; ++t) err = run();
+            cudaEventRecord(e1, s);
+            cudaEventSynchronize(e1);
+            set_pass_variant(n, kKindTc, keep);
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            row.us[v][k] = 1000.0 * ms / 5.0;
+            count_launches(14);
+          }
+          if (err == cudaErrorNotSupported) {
+            err = cudaSuccess;
+            row.us[1][k] = 1e30;
           }
         }
         row.choice[k] = row.us[1][k] < row.us[0][k] ? 1 : 0;

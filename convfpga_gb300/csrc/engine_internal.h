@@ -45,8 +45,13 @@ cudaError_t tc05_init_consts(float2 *tw, cudaStream_t s);
 // Plan table: shape variant (0 / 1) per cube size and pass kind, chosen by the
 // autotuner and recorded in the plan cache.
 // kKindTc: tensor-core kernel of the split-TF32 path (0 tcgen05, 1 mma.sync), N = 256.
+// kKindTcXy: x and y passes of the split-TF32 path on tcgen05, N = 256 (0 separate passes,
+// 1 one pass staged through the L2 scratch ring).
 constexpr int kKindRows = 0, kKindStrided = 1, kKindConv = 2, kKindConvFz = 3, kKindXy = 4, kKindTc = 5,
-              kPassKinds = 6;
+              kKindTcXy = 6, kPassKinds = 7;
+// Tensor-core form of the L2-staged x + y pass (N = 256, tcgen05; xyl2.cu).
+cudaError_t launch_xy_l2_tc_pass(const float2 *src, float2 *dst, int nplanes, bool inverse, float scale,
+                                 const float2 *tw512, cudaStream_t s);
 int pass_kind(int axis, int op);
 void set_pass_variant(int n, int kind, int variant);
 int get_pass_variant(int n, int kind);

@@ -253,6 +253,9 @@ cudaError_t launch_tc05_512_entry(const PassReq &r);
 // L2-staged fused x + y pass for N = 128, 256 or 512 (xyl2.cu, xyl2.cuh).
 cudaError_t launch_xy_l2(int n, const float2 *src, float2 *dst, int nplanes, bool inverse, float scale,
                          const float2 *tw512, unsigned *status, cudaStream_t s);
+// Its tensor-core (split-TF32, tcgen05) form for N = 256 (xyl2.cu, xyl2_tc.cuh).
+cudaError_t launch_xy_l2_tc(const float2 *src, float2 *dst, int nplanes, bool inverse, float scale,
+                            const float2 *tw512, unsigned *status, cudaStream_t s);
 // Fused x + y pass for N = 256 on 8-CTA clusters (passes_n256.cu, xy256.cuh).
 cudaError_t launch_xy256(const float2 *src, float2 *dst, int nplanes, bool inverse, float scale, const float2 *tw512,
                          unsigned int *status, cudaStream_t s);

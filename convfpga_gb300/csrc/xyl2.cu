@@ -1,9 +1,11 @@
-// Launcher of the L2-staged fused x + y pass for N = 128, 256 and 512 (xyl2.cuh): scratch
-// ring per size and dependency counters (grow-only, per process), counters cleared on the
-// stream before every launch, one persistent grid of as many CTAs as fit.
+// Launchers of the L2-staged fused x + y pass for N = 128, 256 and 512 (xyl2.cuh) and of its
+// tensor-core form for N = 256 (xyl2_tc.cuh): scratch ring per size and dependency counters
+// (grow-only, per process), counters cleared on the stream before every launch, one
+// persistent grid of as many CTAs as fit.
 #define CONVGPU_PASS_LAUNCH_IMPL
 #include "pass_launch.cuh"
 #include "xyl2.cuh"
+#include "xyl2_tc.cuh"
 
 #include <algorithm>
 
@@ -145,6 +147,43 @@ cudaError_t launch_xy_l2(int n, const float2 *src, float2 *dst, int nplanes, boo
     case 512: return launch_common<512>(&msrc, nullptr, nullptr, dst, nplanes, inverse, scale, tw512, status, nullptr, s);
     default: return cudaErrorNotSupported;
   }
+}
+
+// Tensor-core (split-TF32, tcgen05) form of launch_xy_l2 for N = 256: same ring, counters
+// and schedule, every 256-point transform on the tensor cores. The engine's twiddle buffer
+// (tw512) must carry the tcgen05 constant block.
+cudaError_t launch_xy_l2_tc(const float2 *src, float2 *dst, int nplanes, bool inverse, float scale,
+                            const float2 *tw512, unsigned *status, cudaStream_t s) {
+  using Cfg = XyL2Cfg<256>;
+  if (nplanes <= 0) return cudaSuccess;
+  if ((reinterpret_cast<uintptr_t>(dst) & 15u) != 0) return cudaErrorNotSupported;
+  CUtensorMap msrc, mscr;
+  if (!encode_rows_map(&msrc, src, 256, (long long)nplanes * 256, Cfg::C)) return cudaErrorNotSupported;
+  int ps, sms;
+  Scratch *ring;
+  cudaError_t e = xy_l2_setup<256>(nplanes, ps, sms, ring);
+  if (e != cudaSuccess) return e;
+  if (!encode_cube_map(&mscr, ring->p, 256, Cfg::RING, 1, Cfg::C)) return cudaErrorNotSupported;
+  static int done[2] = {0, 0};
+  if ((e = set_smem_once(k_xy_l2_tc<false>, kXyTcSmem, done[0])) != cudaSuccess) return e;
+  if ((e = set_smem_once(k_xy_l2_tc<true>, kXyTcSmem, done[1])) != cudaSuccess) return e;
+  static int per_sm = 0;
+  if (per_sm == 0 &&
+      (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)k_xy_l2_tc<false>, kXyTcThreads,
+                                                     kXyTcSmem) != cudaSuccess ||
+       per_sm <= 0)) {
+    cudaGetLastError();
+    per_sm = 1;
+  }
+  unsigned *ctr = reinterpret_cast<unsigned *>(g_ctr.p);
+  const long long ncount = 2LL * nplanes + 2;
+  k_xyl2_clear<<<(unsigned)std::min<long long>((ncount + 255) / 256, 64), 256, 0, s>>>(ctr, ncount);
+  const long long items = 2LL * nplanes * (256 / Cfg::C);
+  const unsigned grid = (unsigned)std::min<long long>(items, (long long)per_sm * sms);
+  auto kern = inverse ? k_xy_l2_tc<true> : k_xy_l2_tc<false>;
+  kern<<<grid, kXyTcThreads, kXyTcSmem, s>>>(msrc, mscr, reinterpret_cast<float2 *>(ring->p), dst, nplanes, scale,
+                                             tw512, ctr, status, Cfg::LAG, Cfg::RING);
+  return cudaGetLastError();
 }
 
 // The same over `ncubes` N^3 cubes at unrelated addresses: rmaps[i] (device memory, from

@@ -160,8 +160,9 @@ int convgpu_autotune(const unsigned *sizes, unsigned count, int write_cache);
  * 1 one pass staged through an L2-resident scratch ring, 2 one pass on 8-CTA clusters;
  * N = 128 and 512: 1 one pass staged through an L2-resident scratch ring;
  * 5 tensor-core kernels of CONVGPU_TENSOR_SPLIT, N = 256: 0 tcgen05 (TMEM accumulators),
- * 1 mma.sync): sets it to set_to (0 or 1; 0..2 for kind 4) when set_to >= 0, and returns
- * the current variant (or a negative CONVGPU_E* code). */
+ * 1 mma.sync; 6 x and y passes of the tcgen05 split path, N = 256: 0 separate passes, 1 one
+ * pass staged through the L2-resident scratch ring): sets it to set_to (0 or 1; 0..2 for
+ * kind 4) when set_to >= 0, and returns the current variant (or a negative CONVGPU_E* code). */
 int convgpu_plan_variant(unsigned N, int kind, int set_to);
 
 /* Waits for the device, then returns and clears the library's device status word in

@@ -137,6 +137,54 @@ def test_tc_host_entry_point(gpu):
     assert rel_l2(ref, out) <= REL_L2_TC
 
 
+@pytest.fixture(params=[0, 1], ids=["separate_xy", "fused_xy"])
+def tc_xy(request, gpu):
+    """x and y passes of the tcgen05 split path: separate, or one pass staged through the
+    L2 scratch ring (plan kind 6)."""
+    keep = (gpu.plan_variant(256, TC_KIND), gpu.plan_variant(256, 6))
+    gpu.plan_variant(256, TC_KIND, 0)
+    gpu.plan_variant(256, 6, request.param)
+    yield request.param
+    gpu.plan_variant(256, TC_KIND, keep[0])
+    gpu.plan_variant(256, 6, keep[1])
+
+
+def test_tc_256_xy_forms_against_fp64(gpu, tc_xy):
+    """Per-signal filters, normalised, two cubes: both forms of the x and y passes are
+    within the bound, and the fused form runs as fused x+y launches (pass slots 12, 13)."""
+    sig, filt, _ = make_config("c256x4")
+    sig, filt = sig[2:4], filt[2:4]
+    flags = gpu.FILTER_PER_SIGNAL | gpu.NORMALIZE | gpu.TENSOR_SPLIT
+    gpu.pass_timing_start()
+    tc = _run(gpu, sig, filt, flags)
+    passes = gpu.pass_timing_read()
+    gpu.pass_timing_stop()
+    ref = conv3d(sig, filt, "fp64", normalize=True, engine="pocketfft")
+    err = rel_l2(ref, tc)
+    print(f"TC x+y {'fused' if tc_xy else 'separate'}: rel-L2 vs FP64 {err:.3e}, max-abs {max_abs(ref, tc):.3e}")
+    assert err <= REL_L2_TC
+    assert ("xy-fwd" in passes and "xy-inv" in passes) == bool(tc_xy)
+    assert gpu.device_status() == 0
+
+
+def test_tc_256_fused_xy_impulse_and_host_entry(gpu, tc_xy):
+    """Position mapping of the fused tensor-core x+y pass (forward and inverse), and the
+    host-buffer entry point on the same plan."""
+    rng = np.random.default_rng(79)
+    n = 256
+    shift = (100, 7, 255)
+    sig = np.zeros((1, n, n, n), np.complex64)
+    sig[0][shift] = 1.0
+    filt = (rng.uniform(-1, 1, (n, n, n)) + 1j * rng.uniform(-1, 1, (n, n, n))).astype(np.complex64)
+    out = _run(gpu, sig, filt, gpu.TENSOR_SPLIT | gpu.NORMALIZE)
+    assert rel_l2(np.roll(filt, shift, axis=(0, 1, 2))[None], out) <= REL_L2_TC
+    sig2 = (rng.standard_normal((2, n, n, n)) + 1j * rng.standard_normal((2, n, n, n))).astype(np.complex64)
+    out2 = np.zeros_like(sig2)
+    t = gpu.conv3d_host(n, sig2, filt, out2, 2, gpu.TENSOR_SPLIT)
+    assert t.valid, gpu.last_error()
+    assert rel_l2(conv3d(sig2, filt, "fp64", engine="pocketfft"), out2) <= REL_L2_TC
+
+
 def _dev(cg, s, f, b, flags):
     o = torch.empty_like(s)
     cg.conv3d_device(s.shape[-1], s, f, o, b, flags)
