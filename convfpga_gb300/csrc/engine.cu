@@ -295,6 +295,13 @@ static cudaError_t pass(int n, int axis, int op, const float2 *src, float2 *dst,
   return e;
 }
 
+// True when the tensor-core path has kernels of its own for size n (N = 256; N = 512 in
+// TF32x3); elsewhere it runs the FP32 kernels, the fused x+y pass included, and its
+// results equal the FP32 path's.
+static bool tc_kernels(int n, int tc) {
+  return tc != 0 && (n == 256 || (n == 512 && tc - 1 == kTcTf32x3));
+}
+
 // Fused x + y pass: for the FP32 path plan kind kKindXy (1 L2-staged (N = 128, 256, 512),
 // 2 8-CTA clusters (N = 256)); for the tensor-core path (tc != 0) the L2-staged pass on
 // tcgen05 (N = 256). Returns cudaErrorNotSupported when it cannot run, in which case the
@@ -308,8 +315,10 @@ static cudaError_t pass_xy(int n, const float2 *src, float2 *dst, int nvol, bool
     cudaEventCreate(&r.b);
     cudaEventRecord(r.a, s);
   }
-  cudaError_t e = tc ? launch_xy_l2_tc_pass(src, dst, nvol * n, inverse, scale, g.tw512, s)
-                     : launch_xy_pass(n, src, dst, nvol * n, inverse, scale, g.tw512, s, get_pass_variant(n, kKindXy));
+  const bool tc_fused = tc_kernels(n, tc);  // else the FP32 pass, also for the tensor-core flag
+  cudaError_t e = tc_fused ? launch_xy_l2_tc_pass(n, src, dst, nvol * n, inverse, scale, g.tw512, s)
+                           : launch_xy_pass(n, src, dst, nvol * n, inverse, scale, g.tw512, s,
+                                            get_pass_variant(n, kKindXy));
   if (g_prof) {
     cudaEventRecord(r.b, s);
     if (e == cudaSuccess) {
@@ -320,16 +329,10 @@ static cudaError_t pass_xy(int n, const float2 *src, float2 *dst, int nvol, bool
     }
   }
   // the L2-staged pass is two launches: counter clear + pass
-  if (e == cudaSuccess) count_launches((tc || get_pass_variant(n, kKindXy) == 1) ? 2 : 1);
+  if (e == cudaSuccess) count_launches((tc_fused || get_pass_variant(n, kKindXy) == 1) ? 2 : 1);
   return e;
 }
 
-// True when the tensor-core path has kernels of its own for size n (N = 256; N = 512 in
-// TF32x3); elsewhere it runs the FP32 kernels, the fused x+y pass included, and its
-// results equal the FP32 path's.
-static bool tc_kernels(int n, int tc) {
-  return tc != 0 && (n == 256 || (n == 512 && tc - 1 == kTcTf32x3));
-}
 static bool use_xy(int n, int tc) {
   if (tc_kernels(n, tc))  // the tcgen05 split-TF32 kernels of N = 256 have a fused form
     return n == 256 && tc - 1 == kTcTf32x3 && get_pass_variant(256, kKindTc) == 0 &&
@@ -1107,7 +1110,7 @@ int bridge_autotune(const unsigned *sizes, unsigned count, int write_cache) {
         if (n == 256) {
           for (int v = 0; v < 2 && err == cudaSuccess; ++v) {
             auto run = [&]() {
-              if (v == 1) return launch_xy_l2_tc_pass(data, data, nvol * n, false, 1.f, g.tw512, s);
+              if (v == 1) return launch_xy_l2_tc_pass(n, data, data, nvol * n, false, 1.f, g.tw512, s);
               cudaError_t r = launch_axis_pass_tc(n, 0, OP_FWD, data, data, nullptr, 0, nvol, 1.f, g.tw512, s,
                                                   kTcTf32x3);
               if (r == cudaSuccess)

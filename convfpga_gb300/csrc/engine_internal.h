@@ -49,8 +49,9 @@ cudaError_t tc05_init_consts(float2 *tw, cudaStream_t s);
 // 1 one pass staged through the L2 scratch ring).
 constexpr int kKindRows = 0, kKindStrided = 1, kKindConv = 2, kKindConvFz = 3, kKindXy = 4, kKindTc = 5,
               kKindTcXy = 6, kPassKinds = 7;
-// Tensor-core form of the L2-staged x + y pass (N = 256, tcgen05; xyl2.cu).
-cudaError_t launch_xy_l2_tc_pass(const float2 *src, float2 *dst, int nplanes, bool inverse, float scale,
+// Tensor-core form of the L2-staged x + y pass (tcgen05; xyl2.cu). It exists for N = 256
+// only: any other n returns cudaErrorNotSupported without launching.
+cudaError_t launch_xy_l2_tc_pass(int n, const float2 *src, float2 *dst, int nplanes, bool inverse, float scale,
                                  const float2 *tw512, cudaStream_t s);
 int pass_kind(int axis, int op);
 void set_pass_variant(int n, int kind, int variant);

@@ -346,9 +346,9 @@ cudaError_t launch_xy_pass(int n, const float2 *src, float2 *dst, int nplanes, b
   return launch_xy_l2(256, src, dst, nplanes, inverse, scale, tw512, device_status_address(), s);
 }
 
-cudaError_t launch_xy_l2_tc_pass(const float2 *src, float2 *dst, int nplanes, bool inverse, float scale,
+cudaError_t launch_xy_l2_tc_pass(int n, const float2 *src, float2 *dst, int nplanes, bool inverse, float scale,
                                  const float2 *tw512, cudaStream_t s) {
-  if (!g_use_tma) return cudaErrorNotSupported;
+  if (n != 256 || !g_use_tma) return cudaErrorNotSupported;
   return launch_xy_l2_tc(src, dst, nplanes, inverse, scale, tw512, device_status_address(), s);
 }
 
