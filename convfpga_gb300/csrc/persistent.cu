@@ -486,6 +486,11 @@ cudaError_t build_plan(PPlan &p, const float2 *tw512, unsigned *status) {
   if ((e = cudaFuncSetAttribute(k_persistent_queue, cudaFuncAttributeMaxDynamicSharedMemorySize, kPSmemBytes)) !=
       cudaSuccess)
     return e;
+  // The occupancy query follows the kernel's carveout preference: ask for the largest
+  // shared-memory share so that it counts the CTAs the launch can actually hold.
+  if ((e = cudaFuncSetAttribute(k_persistent_queue, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                cudaSharedmemCarveoutMaxShared)) != cudaSuccess)
+    return e;
   int dev = 0, sms = 0, per_sm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -600,7 +605,9 @@ cudaError_t launch_small_conv(int n, const float2 *sig, const float2 *filt, floa
     grid_dev = dev;
   }
   if (grid_of[ai] == 0 &&
-      (e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kPSmemBytes)) != cudaSuccess)
+      ((e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kPSmemBytes)) != cudaSuccess ||
+       (e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 cudaSharedmemCarveoutMaxShared)) != cudaSuccess))
     return e;
   if (grid_of[ai] == 0) {
     int sms = 0, per_sm = 0;

@@ -165,15 +165,26 @@ cudaError_t launch_xy_l2_tc(const float2 *src, float2 *dst, int nplanes, bool in
   if (e != cudaSuccess) return e;
   if (!encode_cube_map(&mscr, ring->p, 256, Cfg::RING, 1, Cfg::C)) return cudaErrorNotSupported;
   static int done[2] = {0, 0};
-  if ((e = set_smem_once(k_xy_l2_tc<false>, kXyTcSmem, done[0])) != cudaSuccess) return e;
-  if ((e = set_smem_once(k_xy_l2_tc<true>, kXyTcSmem, done[1])) != cudaSuccess) return e;
+  for (int i = 0; i < 2; ++i) {
+    if (done[i]) continue;
+    auto kern = i ? k_xy_l2_tc<true> : k_xy_l2_tc<false>;
+    if ((e = set_smem_once(kern, kXyTcSmem, done[i])) != cudaSuccess) return e;
+    if ((e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                  cudaSharedmemCarveoutMaxShared)) != cudaSuccess)
+      return e;
+  }
+  // CTAs per SM from the footprint: shared memory (the kernel plus the driver's reserve
+  // per block) against the SM's, at most the kXyTcMinBlocks the register budget was
+  // compiled for. (Without a carveout preference the occupancy query returned 1 for this
+  // kernel; ncu reports 5 as the shared-memory limit of the launch.) Any number is correct:
+  // the schedule needs no co-residency.
   static int per_sm = 0;
-  if (per_sm == 0 &&
-      (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)k_xy_l2_tc<false>, kXyTcThreads,
-                                                     kXyTcSmem) != cudaSuccess ||
-       per_sm <= 0)) {
-    cudaGetLastError();
-    per_sm = 1;
+  if (per_sm == 0) {
+    int dev = 0, smem_sm = 0, reserve = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    cudaDeviceGetAttribute(&reserve, cudaDevAttrReservedSharedMemoryPerBlock, dev);
+    per_sm = std::max(1, std::min(kXyTcMinBlocks, smem_sm / (kXyTcSmem + reserve)));
   }
   unsigned *ctr = reinterpret_cast<unsigned *>(g_ctr.p);
   const long long ncount = 2LL * nplanes + 2;
