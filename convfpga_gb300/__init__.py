@@ -314,7 +314,7 @@ def pass_timing_read() -> dict:
     return out
 
 
-PLAN_KINDS = ("rows", "strided", "conv", "conv_fz", "xy", "tc", "tcxy")
+PLAN_KINDS = ("rows", "strided", "conv", "conv_fz", "xy", "tc", "tcxy", "herm")
 
 
 def autotune(sizes, write_cache: bool = True) -> None:

@@ -366,6 +366,44 @@ static cudaError_t pass_real(int n, const float *filt, float2 *spec, int count, 
   return e;
 }
 
+// Hermitian half spectra of real filters (FP32 path, N >= 64, plan kind kKindHalf = 1).
+static bool use_half(unsigned n, bool real, int tc) {
+  return real && tc == 0 && half_spectrum_pitch((int)n) > 0 && get_pass_variant((int)n, kKindHalf) == 1;
+}
+
+// A pass over (or into, or against) a half spectrum, profiled in its axis/op slot with the
+// bytes it moves: axis 0 reads N^3 floats and writes N^2 W values; axes 1 and 2 read and
+// write N^2 W values; the paired fused z pass reads and writes the signal and reads a
+// (C+2)/(2C) share of a full spectrum's bytes (C = 16 columns per tile below N = 256, 8 above).
+static cudaError_t pass_half(int n, int axis, int op, const void *src, float2 *dst, const float2 *filt,
+                             long long filt_vol, int nvol, float scale, cudaStream_t s) {
+  PassRec r{axis * 4 + op, 0.0, nullptr, nullptr};
+  if (g_prof) {
+    const double v = (double)n * n * n, h = (double)n * n * half_spectrum_pitch(n);
+    const double cols = n >= 256 ? 8.0 : 16.0;
+    r.bytes = nvol * (axis == 0 ? 4.0 * v + 8.0 * h
+                                : (op == OP_CONV ? 16.0 * v + 8.0 * v * (cols + 2.0) / (2.0 * cols) : 16.0 * h));
+    cudaEventCreate(&r.a);
+    cudaEventCreate(&r.b);
+    cudaEventRecord(r.a, s);
+  }
+  const cudaError_t e = launch_axis_pass_half(n, axis, op, src, dst, filt, filt_vol, nvol, scale, g.tw512, s);
+  if (g_prof) {
+    cudaEventRecord(r.b, s);
+    g_prof_recs.push_back(r);
+  }
+  return e;
+}
+
+// Half spectra of `count` real filters (N^3 floats each) into spec (N^2 W values each):
+// x pass of the real rows, then y and z passes over the half width.
+static cudaError_t enqueue_filter_half(int n, const float *filt, float2 *spec, int count, cudaStream_t s) {
+  CG_TRY(pass_half(n, 0, OP_FWD, filt, spec, nullptr, 0, count, 1.f, s));
+  CG_TRY(pass_half(n, 1, OP_FWD, spec, spec, nullptr, 0, count, 1.f, s));
+  CG_TRY(pass_half(n, 2, OP_FWD, spec, spec, nullptr, 0, count, 1.f, s));
+  return cudaSuccess;
+}
+
 // Filter spectra of `count` filters (x, y and, unless xy_only, z passes) into spec. With
 // `real`, filt holds N^3 floats per filter (CONVGPU_FILTER_REAL); spec must not overlap it.
 static cudaError_t enqueue_filter(int n, const float2 *filt, float2 *spec, int count, bool xy_only,
@@ -384,11 +422,11 @@ static cudaError_t enqueue_filter(int n, const float2 *filt, float2 *spec, int c
   return cudaSuccess;
 }
 
-// Signal passes. fop: OP_CONV (spec is a full spectrum) or OP_CONV_FZ (xy only).
-// mid (optional) is recorded after the fused z pass.
+// Signal passes. fop: OP_CONV (spec is a full spectrum, or with `half` a Hermitian half
+// spectrum) or OP_CONV_FZ (xy only). mid (optional) is recorded after the fused z pass.
 static cudaError_t enqueue_signals(int n, const float2 *sig, float2 *out, const float2 *spec,
                                    long long spec_vol, int fop, int nsig, float scale, cudaStream_t s,
-                                   cudaEvent_t mid, int tc = 0) {
+                                   cudaEvent_t mid, int tc = 0, bool half = false) {
   cudaError_t xe = use_xy(n, tc) ? pass_xy(n, sig, out, nsig, false, 1.f, s, tc) : cudaErrorNotSupported;
   if (xe != cudaSuccess && xe != cudaErrorNotSupported) return xe;
   const bool fused = xe == cudaSuccess;
@@ -396,7 +434,10 @@ static cudaError_t enqueue_signals(int n, const float2 *sig, float2 *out, const 
     CG_TRY(pass(n, 0, OP_FWD, sig, out, nullptr, 0, nsig, 1.f, s, tc));
     CG_TRY(pass(n, 1, OP_FWD, out, out, nullptr, 0, nsig, 1.f, s, tc));
   }
-  CG_TRY(pass(n, 2, fop, out, out, spec, spec_vol, nsig, 1.f, s, tc));
+  if (half)
+    CG_TRY(pass_half(n, 2, OP_CONV, out, out, spec, spec_vol, nsig, 1.f, s));
+  else
+    CG_TRY(pass(n, 2, fop, out, out, spec, spec_vol, nsig, 1.f, s, tc));
   if (mid) cudaEventRecord(mid, s);
   if (fused) {
     const cudaError_t e = pass_xy(n, out, out, nsig, true, scale, s, tc);
@@ -408,9 +449,17 @@ static cudaError_t enqueue_signals(int n, const float2 *sig, float2 *out, const 
   return cudaSuccess;
 }
 
+static int tc_of(unsigned flags) {
+  // 0: FP32 kernels; 1 + split precision for the tensor-core path.
+  return (flags & (kFlagTensorSplit | kFlagTensorBf16x3)) ? 1 + ((flags & kFlagTensorBf16x3) ? kTcBf16x3 : kTcTf32x3)
+                                                          : 0;
+}
+
 static size_t workspace_bytes_for(unsigned n, unsigned how_many, unsigned flags) {
-  const size_t vol = (size_t)n * n * n * sizeof(float2);
+  size_t vol = (size_t)n * n * n * sizeof(float2);
   if (flags & kFlagFilterIsSpectrum) return 0;
+  if (use_half(n, (flags & kFlagFilterReal) != 0, tc_of(flags)))
+    vol = (size_t)n * n * half_spectrum_pitch((int)n) * sizeof(float2);  // a half spectrum per filter
   if (flags & kFlagPerSignalFilter) return vol * how_many;
   return vol;
 }
@@ -424,10 +473,7 @@ static cudaError_t enqueue_conv_device(unsigned n, const float2 *sig, const floa
                                        unsigned how_many, unsigned flags, float2 *ws, cudaStream_t s) {
   const float scale = (flags & kFlagNormalize) ? (float)(1.0 / ((double)n * n * n)) : 1.0f;
   const long long V = (long long)n * n * n;
-  // 0: FP32 kernels; 1 + split precision for the tensor-core path.
-  const int tc = (flags & (kFlagTensorSplit | kFlagTensorBf16x3))
-                     ? 1 + ((flags & kFlagTensorBf16x3) ? kTcBf16x3 : kTcTf32x3)
-                     : 0;
+  const int tc = tc_of(flags);
   if (flags & kFlagFilterIsSpectrum) {
     const long long sv = (flags & kFlagPerSignalFilter) ? V : 0;
     return enqueue_signals(n, sig, out, filt, sv, OP_CONV, how_many, scale, s, nullptr, tc);
@@ -443,6 +489,13 @@ static cudaError_t enqueue_conv_device(unsigned n, const float2 *sig, const floa
       return cudaSuccess;
     }
     cudaGetLastError();  // not applicable (size, residency): the per-pass launches below
+  }
+  if (use_half(n, real, tc)) {  // Hermitian half spectra, every signal through the paired z pass
+    const bool per = (flags & kFlagPerSignalFilter) != 0;
+    cudaError_t e = enqueue_filter_half((int)n, reinterpret_cast<const float *>(filt), ws, per ? (int)how_many : 1, s);
+    if (e != cudaSuccess) return e;
+    const long long hv = (long long)n * n * half_spectrum_pitch((int)n);
+    return enqueue_signals(n, sig, out, ws, per ? hv : 0, OP_CONV, how_many, scale, s, nullptr, 0, true);
   }
   if (flags & kFlagPerSignalFilter) {
     cudaError_t e = enqueue_filter(n, filt, ws, how_many, true, s, tc, real);
@@ -600,9 +653,14 @@ int bridge_conv_uneven_device(const UnevenJob *jobs, unsigned njobs, const void 
     set_err(bad);
     return kErrInval;
   }
-  if (flags & kFlagFilterReal) {
-    set_err("CONVGPU_FILTER_REAL is not supported by the uneven-batch entry point");
+  const bool real = (flags & kFlagFilterReal) != 0;  // filter offsets then count floats
+  if (real && !(flags & kFlagUnevenPerJob)) {
+    set_err("CONVGPU_FILTER_REAL in an uneven batch needs CONVGPU_UNEVEN_PER_JOB");
     return kErrUnsupported;
+  }
+  if (real && (flags & kFlagFilterIsSpectrum)) {
+    set_err("CONVGPU_FILTER_REAL and CONVGPU_FILTER_IS_SPECTRUM exclude each other");
+    return kErrInval;
   }
   std::lock_guard<std::recursive_mutex> lk(g.mu);
   int rc = ensure_init_locked();
@@ -633,7 +691,12 @@ int bridge_conv_uneven_device(const UnevenJob *jobs, unsigned njobs, const void 
   CallOrder order((cudaStream_t)stream);
   for (unsigned j = 0; j < njobs; ++j) {
     const float2 *s = (const float2 *)d_sig + jobs[j].sig_off;
-    const float2 *f = (const float2 *)d_filt + jobs[j].filt_off;
+    const float2 *f = real ? reinterpret_cast<const float2 *>((const float *)d_filt + jobs[j].filt_off)
+                           : (const float2 *)d_filt + jobs[j].filt_off;
+    if (real && (reinterpret_cast<uintptr_t>(f) & 3u)) {
+      set_err("a real filter must be 4-byte aligned");
+      return kErrInval;
+    }
     float2 *o = (float2 *)d_out + jobs[j].out_off;
     e = enqueue_conv_device(jobs[j].n, s, f, o, 1, flags & ~kFlagPerSignalFilter, (float2 *)g.ws.p,
                             (cudaStream_t)stream);
@@ -825,10 +888,7 @@ Timing bridge_conv_host(unsigned n, const void *sig, const void *filt, void *out
     set_err("CONVGPU_FILTER_IS_SPECTRUM is not supported by the host-buffer entry points");
     return t;
   }
-  // 0: FP32 kernels; 1 + split precision for the tensor-core path.
-  const int tc = (flags & (kFlagTensorSplit | kFlagTensorBf16x3))
-                     ? 1 + ((flags & kFlagTensorBf16x3) ? kTcBf16x3 : kTcTf32x3)
-                     : 0;
+  const int tc = tc_of(flags);
   std::lock_guard<std::recursive_mutex> lk(g.mu);
   if (ensure_init_locked() != 0) return t;
   (void)mode;
@@ -893,7 +953,9 @@ Timing bridge_conv_host(unsigned n, const void *sig, const void *filt, void *out
   for (unsigned b = 0; b < nbuf; ++b) freed[b] = pool.get();
 
   float2 *fspec = (float2 *)g.hfilt.p;
-  const int key = tc + (real ? 8 : 0);  // path of the kept spectrum
+  const bool half = use_half(n, real, tc);  // real filters as Hermitian half spectra
+  const long long hv = half ? (long long)n * n * half_spectrum_pitch((int)n) : 0;
+  const int key = tc + (real ? 8 : 0) + (half ? 16 : 0);  // path of the kept spectrum
   const bool cached = filter_cache_hit(filt, n, key, flags, per_signal);
   if (!per_signal && !cached) {
     float2 *fin = real ? (float2 *)g.hreal[3].p : fspec;
@@ -901,7 +963,9 @@ Timing bridge_conv_host(unsigned n, const void *sig, const void *filt, void *out
     e = cudaMemcpyAsync(fin, filt, fbytes, cudaMemcpyHostToDevice, g.sh2d);
     cudaEventRecord(f1, g.sh2d);
     cudaStreamWaitEvent(g.sc, f1, 0);
-    if (e == cudaSuccess) e = enqueue_filter(n, fin, fspec, 1, false, g.sc, tc, real);
+    if (e == cudaSuccess)
+      e = half ? enqueue_filter_half(n, (const float *)fin, fspec, 1, g.sc)
+               : enqueue_filter(n, fin, fspec, 1, false, g.sc, tc, real);
     cudaEventRecord(f2, g.sc);
     if (e == cudaSuccess) filter_cache_set(filt, n, key, flags, per_signal);
   }
@@ -941,15 +1005,16 @@ Timing bridge_conv_host(unsigned n, const void *sig, const void *filt, void *out
     cudaStreamWaitEvent(g.sc, per_signal ? hf[c] : h1[c], 0);
     cudaEventRecord(c0[c], g.sc);
     if (per_signal) {
-      e = enqueue_filter(n, (const float2 *)fin, (float2 *)g.hfio[b].p, cnt, true, g.sc, tc, real);
+      e = half ? enqueue_filter_half(n, (const float *)fin, (float2 *)g.hfio[b].p, (int)cnt, g.sc)
+               : enqueue_filter(n, (const float2 *)fin, (float2 *)g.hfio[b].p, cnt, true, g.sc, tc, real);
       cudaEventRecord(cf[c], g.sc);
       cudaStreamWaitEvent(g.sc, h1[c], 0);
       cudaEventRecord(cs[c], g.sc);  // compute time excludes the wait for the signals' upload
       if (e == cudaSuccess)
-        e = enqueue_signals(n, io, io, (const float2 *)g.hfio[b].p, (long long)V, OP_CONV_FZ, cnt, scale, g.sc,
-                            cm[c], tc);
+        e = enqueue_signals(n, io, io, (const float2 *)g.hfio[b].p, half ? hv : (long long)V,
+                            half ? OP_CONV : OP_CONV_FZ, cnt, scale, g.sc, cm[c], tc, half);
     } else {
-      e = enqueue_signals(n, io, io, fspec, 0, OP_CONV, cnt, scale, g.sc, cm[c], tc);
+      e = enqueue_signals(n, io, io, fspec, 0, OP_CONV, cnt, scale, g.sc, cm[c], tc, half);
     }
     cudaEventRecord(c1[c], g.sc);
   }
@@ -995,7 +1060,7 @@ Timing bridge_conv_host(unsigned n, const void *sig, const void *filt, void *out
 // (src/fft_conv3D.cpp:85-112): one line per cube size with the shape variant chosen for
 // each pass kind and the timings (microseconds per launch, variants 0 and 1) it was
 // chosen from.
-static const char *kKindNames[kPassKinds] = {"rows", "strided", "conv", "conv_fz", "xy", "tc", "tcxy"};
+static const char *kKindNames[kPassKinds] = {"rows", "strided", "conv", "conv_fz", "xy", "tc", "tcxy", "herm"};
 
 static void load_plan_cache(const std::string &path) {
   FILE *f = std::fopen(path.c_str(), "r");
@@ -1100,6 +1165,36 @@ int bridge_autotune(const unsigned *sizes, unsigned count, int write_cache) {
           }
         }
         row.choice[k] = row.us[1][k] < row.us[0][k] ? 1 : 0;
+        set_pass_variant(n, k, row.choice[k]);
+        continue;
+      }
+      if (k == kKindHalf) {
+        // fused z pass of real filters: full spectrum (variant 0, the chosen conv shape)
+        // against the paired pass over a Hermitian half spectrum (variant 1); a tie goes
+        // to the half spectrum, whose filter transform also moves fewer bytes
+        for (int v = 0; v < 2; ++v) row.us[v][k] = 0.0;
+        if (half_spectrum_pitch(n) > 0) {
+          for (int v = 0; v < 2 && err == cudaSuccess; ++v) {
+            auto run = [&]() {
+              return v ? launch_axis_pass_half(n, 2, OP_CONV, data, data, spec, 0, nvol, 1.f, g.tw512, s)
+                       : launch_axis_pass(n, 2, OP_CONV, data, data, spec, 0, nvol, 1.f, g.tw512, s);
+            };
+            for (int w = 0; w < 2 && err == cudaSuccess; ++w) err = run();
+            cudaEventRecord(e0, s);
+            for (int t = 0; t < 5 && err == cudaSuccess; ++t) err = run();
+            cudaEventRecord(e1, s);
+            cudaEventSynchronize(e1);
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            row.us[v][k] = 1000.0 * ms / 5.0;
+            count_launches(7);
+          }
+          if (err == cudaErrorNotSupported) {
+            err = cudaSuccess;
+            row.us[1][k] = 1e30;
+          }
+        }
+        row.choice[k] = (half_spectrum_pitch(n) > 0 && row.us[1][k] <= 1.02 * row.us[0][k]) ? 1 : 0;
         set_pass_variant(n, k, row.choice[k]);
         continue;
       }

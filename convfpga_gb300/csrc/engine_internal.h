@@ -24,6 +24,17 @@ cudaError_t launch_axis_pass(int n, int axis, int op, const float2 *src, float2 
 cudaError_t launch_axis_pass_real(int n, const float *src, float2 *dst, int nvol, const float2 *tw512,
                                   cudaStream_t s);
 
+// Hermitian half spectra of real filters (herm.cuh), N >= 64: axis 0 (OP_FWD) transforms
+// real rows (src: N^3 floats per cube) into the half layout of pitch half_spectrum_pitch(n)
+// (N * N * pitch values per cube); axis 1 / 2 (OP_FWD) transform that layout in place;
+// axis 2 OP_CONV runs the signals' paired fused z pass against a half spectrum `filt`
+// (filt_vol_elems: 0 shared, N*N*pitch per signal). cudaErrorNotSupported below N = 64
+// or when tensor maps cannot describe the operands.
+cudaError_t launch_axis_pass_half(int n, int axis, int op, const void *src, float2 *dst, const float2 *filt,
+                                  long long filt_vol_elems, int nvol, float scale, const float2 *tw512,
+                                  cudaStream_t s);
+int half_spectrum_pitch(int n);
+
 // Split precision of the tensor-core path.
 constexpr int kTcTf32x3 = 0;
 constexpr int kTcBf16x3 = 1;
@@ -47,8 +58,10 @@ cudaError_t tc05_init_consts(float2 *tw, cudaStream_t s);
 // kKindTc: tensor-core kernel of the split-TF32 path (0 tcgen05, 1 mma.sync), N = 256.
 // kKindTcXy: x and y passes of the split-TF32 path on tcgen05, N = 256 (0 separate passes,
 // 1 one pass staged through the L2 scratch ring).
+// kKindHalf: spectra of real filters (CONVGPU_FILTER_REAL), N >= 64: 0 full, 1 Hermitian
+// half spectra with the paired fused z pass (herm.cuh).
 constexpr int kKindRows = 0, kKindStrided = 1, kKindConv = 2, kKindConvFz = 3, kKindXy = 4, kKindTc = 5,
-              kKindTcXy = 6, kPassKinds = 7;
+              kKindTcXy = 6, kKindHalf = 7, kPassKinds = 8;
 // Tensor-core form of the L2-staged x + y pass (tcgen05; xyl2.cu). It exists for N = 256
 // only: any other n returns cudaErrorNotSupported without launching.
 cudaError_t launch_xy_l2_tc_pass(int n, const float2 *src, float2 *dst, int nplanes, bool inverse, float scale,

@@ -13,6 +13,7 @@
 #include <cstdint>
 #include <cstring>
 
+#include "herm.cuh"
 #include "passes.cuh"
 
 namespace convgpu {
@@ -43,6 +44,7 @@ struct PassReq {
   int nplanes;  // x / y passes: planes of N*N points to transform (a cube is N planes)
   int variant;  // shape variant 0 / 1
   bool real_src;  // x pass of real rows (a.src holds floats): k_rows_real
+  int half;       // Hermitian half-spectrum layout of pitch half_pitch(N) (herm.cuh), else 0
   PassArgs a;
   cudaStream_t s;
 };
@@ -52,6 +54,8 @@ constexpr int kModeTma = 0, kModeTable = 1, kModeGather = 2;
 bool encode_cube_map(CUtensorMap *m, const void *base, int n, long long nplanes, int axis, int cols);
 bool encode_rows_map(CUtensorMap *m, const void *base, int n, long long rows, int xc);
 bool encode_rows512_map(CUtensorMap *m, const void *base, long long rows, int xc);
+// As encode_cube_map over planes of N rows of `width` complex values (row pitch = width).
+bool encode_pitched_map(CUtensorMap *m, const void *base, int width, int n, long long nplanes, int axis, int cols);
 
 template <int N>
 cudaError_t launch_size(const PassReq &r);
@@ -204,8 +208,68 @@ static cudaError_t launch_rows_real(const PassReq &r) {
   return cudaGetLastError();
 }
 
+// Passes over Hermitian half spectra (herm.cuh), N >= 64, shape variant 1's radix plan and
+// columns: the real filter's x pass storing the first W = half_pitch(N) values of every row
+// (axis 0), its y / z passes over that width (OP_FWD), and the paired fused z pass of the
+// signals against it (axis 2, OP_CONV).
+template <int N>
+static cudaError_t launch_half(const PassReq &r) {
+  if constexpr (half_pitch(N) == 0) {
+    return cudaErrorNotSupported;
+  } else {
+    using S = Shape<N, 1>;
+    constexpr int E = S::E, COLS = S::SC, W = half_pitch(N);
+    static_assert(W % COLS == 0 && (N / 2) % COLS == 0 && (COLS + 2) * 8 % 16 == 0, "half-layout tiles");
+    PassArgs a = r.a;
+    if ((reinterpret_cast<uintptr_t>(a.dst) & 15u) != 0) return cudaErrorNotSupported;
+    if (r.axis == 0) {
+      if (!r.real_src || r.op != OP_FWD) return cudaErrorInvalidValue;
+      PassReq q = r;
+      q.a.out_cols = W;
+      return r.variant ? launch_rows_real<N, 1>(q) : launch_rows_real<N, 0>(q);
+    }
+    if (r.op == OP_FWD) {
+      auto kern = k_strided_tma<N, E, COLS, OP_FWD, typename S::Plan>;
+      constexpr int smem = tma_pass_smem_bytes<N, COLS, OP_FWD>();
+      static int done = 0;
+      cudaError_t e = set_smem_once(kern, smem, done);
+      if (e != cudaSuccess) return e;
+      CUtensorMap m;
+      if (!encode_pitched_map(&m, a.src, W, N, (long long)r.nvol * N, r.axis, COLS)) return cudaErrorNotSupported;
+      a.vol_elems = (long long)N * N * W;
+      a.groups_x = W / COLS;
+      a.groups_per_vol = N * a.groups_x;
+      a.axis_stride = r.axis == 1 ? W : (long long)N * W;
+      a.plane_pitch = r.axis == 1 ? (long long)N * W : W;
+      const long long blocks = (long long)r.nvol * a.groups_per_vol;
+      if (blocks <= 0 || blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+      kern<<<(unsigned)blocks, COLS * (N / E), smem, r.s>>>(m, m, a, r.axis);
+      return cudaGetLastError();
+    }
+    if (r.op == OP_CONV && r.axis == 2) {
+      auto kern = k_zconv_half<N, E, COLS, typename S::Plan>;
+      constexpr int smem = zconv_half_smem_bytes<N, COLS>();
+      static int done = 0;
+      cudaError_t e = set_smem_once(kern, smem, done);
+      if (e != cudaSuccess) return e;
+      CUtensorMap ms, mh;
+      const long long fplanes = a.filt_vol_elems ? (long long)r.nvol * N : (long long)N;
+      if (!encode_cube_map(&ms, a.src, N, (long long)r.nvol * N, 2, COLS) ||
+          !encode_pitched_map(&mh, a.filt, W, N, fplanes, 2, COLS + 2))
+        return cudaErrorNotSupported;
+      a.vol_elems = (long long)N * N * N;
+      const long long blocks = (long long)r.nvol * N * (N / 2 / COLS);
+      if (blocks <= 0 || blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+      kern<<<(unsigned)blocks, 2 * COLS * (N / E), smem, r.s>>>(ms, mh, a);
+      return cudaGetLastError();
+    }
+    return cudaErrorInvalidValue;
+  }
+}
+
 template <int N>
 cudaError_t launch_size(const PassReq &r) {
+  if (r.half) return launch_half<N>(r);
   if (r.real_src) return r.variant ? launch_rows_real<N, 1>(r) : launch_rows_real<N, 0>(r);
   if (r.mode == kModeGather) return launch_gather_op<N>(r);
   if (r.mode == kModeTable) return launch_tma_variant<N, 0>(r);  // tables are encoded with variant 0

@@ -53,6 +53,23 @@ static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
   return fn;
 }
 
+// Tensor map over `nplanes` consecutive planes of n rows of `width` complex64 values
+// (8-byte elements), dims (x, y, plane) = (width, n, nplanes); box {cols, 1 or nbox,
+// nbox or 1}.
+bool encode_pitched_map(CUtensorMap *m, const void *base, int width, int n, long long nplanes, int axis, int cols) {
+  auto enc = tensor_map_encoder();
+  if (!enc || (reinterpret_cast<uintptr_t>(base) & 15u) != 0 || nplanes > 0x7fffffffLL || (width & 1)) return false;
+  const cuuint32_t nbox = (cuuint32_t)(n > 256 ? 256 : n);
+  cuuint64_t dims[3] = {(cuuint64_t)width, (cuuint64_t)n, (cuuint64_t)nplanes};
+  cuuint64_t strides[2] = {(cuuint64_t)width * 8, (cuuint64_t)width * n * 8};
+  cuuint32_t box[3] = {(cuuint32_t)cols, axis == 1 ? nbox : 1u, axis == 1 ? 1u : nbox};
+  cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_UINT64, 3, const_cast<void *>(base), dims, strides, box, estr,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
 // Tensor map over `nplanes` consecutive N x N planes of complex64 (8-byte elements),
 // dims (x, y, plane) = (N, N, nplanes); box {cols, 1 or nbox, nbox or 1}.
 bool encode_cube_map(CUtensorMap *m, const void *base, int n, long long nplanes, int axis, int cols) {
@@ -304,6 +321,27 @@ cudaError_t launch_axis_pass_real(int n, const float *src, float2 *dst, int nvol
   r.s = s;
   return dispatch(n, r);
 }
+
+cudaError_t launch_axis_pass_half(int n, int axis, int op, const void *src, float2 *dst, const float2 *filt,
+                                  long long filt_vol_elems, int nvol, float scale, const float2 *tw512,
+                                  cudaStream_t s) {
+  if (nvol <= 0) return cudaSuccess;
+  if (size_index(n) < 0 || half_pitch(n) == 0 || !g_use_tma) return cudaErrorNotSupported;
+  PassReq r{};
+  r.mode = kModeTma;
+  r.axis = axis;
+  r.op = op;
+  r.nvol = nvol;
+  r.nplanes = nvol * n;
+  r.variant = get_pass_variant(n, kKindRows);
+  r.real_src = axis == 0;
+  r.half = half_pitch(n);
+  r.a = make_args(n, reinterpret_cast<const float2 *>(src), dst, filt, filt_vol_elems, scale, tw512);
+  r.s = s;
+  return dispatch(n, r);
+}
+
+int half_spectrum_pitch(int n) { return half_pitch(n); }
 
 cudaError_t launch_axis_pass_tc(int n, int axis, int op, const float2 *src, float2 *dst, const float2 *filt,
                                 long long filt_vol_elems, int nvol, float scale, const float2 *tw512,

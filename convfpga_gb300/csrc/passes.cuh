@@ -50,6 +50,9 @@ struct PassArgs {
   float2 *const *dsts;
   // Device status word: kernels OR in kStatus* bits when a bounded wait gives up.
   unsigned int *status;
+  // x pass of real rows only: values stored per row, at that row pitch (0: all N). The
+  // Hermitian half spectrum of a real filter keeps the first half_pitch(N) (herm.cuh).
+  int out_cols;
 };
 
 // Shared-memory slot of pencil position n for the two layouts.
@@ -193,7 +196,8 @@ __global__ void __launch_bounds__(COLS *(N / E)) k_axis_pass(PassArgs a) {
 
 // x pass of real rows (real filters): a.src holds N floats per row; each value enters the
 // transform as (x, 0). Same radix plan and exchange layout as k_rows_tma, so the result
-// equals the complex x pass of the same data with zero imaginary parts, bit for bit.
+// equals the complex x pass of the same data with zero imaginary parts, bit for bit. With
+// a.out_cols it stores only the first out_cols values of each row, at that pitch.
 template <int N, int E, int XC, class Plan>
 __global__ void __launch_bounds__(XC *(N / E)) k_rows_real(PassArgs a) {
   constexpr int T = N / E;
@@ -209,9 +213,11 @@ __global__ void __launch_bounds__(XC *(N / E)) k_rows_real(PassArgs a) {
   for (int e = 0; e < E; ++e) v[e] = make_float2(src[t + e * T], 0.f);
   __syncthreads();  // twiddle table ready
   fft_forward<N, E>(v, t, tw, sm, RowSlot<N>{c * row_pitch<N>()}, Plan{});
-  float2 *dst = a.dst + row * N + t;
+  const int w = a.out_cols ? a.out_cols : N;
+  float2 *dst = a.dst + row * w + t;
 #pragma unroll
-  for (int e = 0; e < E; ++e) dst[e * T] = v[e];
+  for (int e = 0; e < E; ++e)
+    if (t + e * T < w) dst[e * T] = v[e];
 }
 
 // Dynamic shared memory of the TMA-fed x pass: barrier slot, the unpadded row tile (TMA

@@ -114,7 +114,8 @@ typedef struct {
  * 4096 jobs), also replayed from a cached graph. Graphs and filter-spectrum workspaces
  * stay allocated until fpga_final. With CONVGPU_UNEVEN_PER_JOB, CONVGPU_TENSOR_SPLIT,
  * CONVGPU_FILTER_IS_SPECTRUM, or cubes not 16-byte aligned, the jobs run one after
- * another through the per-size pass kernels. */
+ * another through the per-size pass kernels. CONVGPU_FILTER_REAL (filters as N^3 floats,
+ * filter offsets counted in floats) needs CONVGPU_UNEVEN_PER_JOB. */
 int convgpu_conv3d_uneven_device(const convgpu_job *jobs, unsigned njobs, const float2 *d_sig_base,
                                  const float2 *d_filter_base, float2 *d_out_base, unsigned flags, void *stream);
 
@@ -161,8 +162,11 @@ int convgpu_autotune(const unsigned *sizes, unsigned count, int write_cache);
  * N = 128 and 512: 1 one pass staged through an L2-resident scratch ring;
  * 5 tensor-core kernels of CONVGPU_TENSOR_SPLIT, N = 256: 0 tcgen05 (TMEM accumulators),
  * 1 mma.sync; 6 x and y passes of the tcgen05 split path, N = 256: 0 separate passes, 1 one
- * pass staged through the L2-resident scratch ring): sets it to set_to (0 or 1; 0..2 for
- * kind 4) when set_to >= 0, and returns the current variant (or a negative CONVGPU_E* code). */
+ * pass staged through the L2-resident scratch ring; 7 spectra of real filters
+ * (CONVGPU_FILTER_REAL, FP32 path, N >= 64): 0 full spectra, 1 Hermitian half spectra, kx up
+ * to N/2 only, with a fused z pass that serves a column tile and its mirror from one read):
+ * sets it to set_to (0 or 1; 0..2 for kind 4) when set_to >= 0, and returns the current
+ * variant (or a negative CONVGPU_E* code). */
 int convgpu_plan_variant(unsigned N, int kind, int set_to);
 
 /* Waits for the device, then returns and clears the library's device status word in

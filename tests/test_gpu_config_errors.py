@@ -6,6 +6,8 @@ workload, path, relative L2 error, max-abs error, and max |reference|.
     and max-abs < 1e-5 * max |reference|.
   - Tensor-core split path (CONVGPU_TENSOR_SPLIT, TF32x3): rel-L2 <= 1e-5 at 256^3 and 512^3,
     both of which have tensor-core kernels (the result differs from the FP32 path's).
+  - The workloads with real Gaussian filters (128^3 x8, the uneven batch, 512^3 x1) also
+    through Hermitian half spectra (plan kind 7 = 1): FP32 bounds as above.
 Inputs are the workloads' seeded synthetic cubes (oracle.make_config), with the
 workloads' options: 64^3 normalised by 1/N^3, shared real Gaussian filters passed as real
 (CONVGPU_FILTER_REAL), per-signal filters at 256^3, one filter per job in the uneven batch.
@@ -40,6 +42,48 @@ def _device(cg, sig, filt, flags, real):
     del s, f, o
     torch.cuda.empty_cache()
     return out
+
+
+@pytest.fixture
+def half_spectra(gpu):
+    keep = {n: gpu.plan_variant(n, 7) for n in (64, 128, 256, 512)}
+    for n in keep:
+        gpu.plan_variant(n, 7, 1)
+    yield
+    for n, v in keep.items():
+        gpu.plan_variant(n, 7, v)
+
+
+@pytest.mark.parametrize("name", ["c128x8", "c512x1"])
+def test_real_filter_workloads_half_spectra_against_fp64(gpu, half_spectra, name):
+    sig, filt, _ = make_config(name)
+    ref = conv3d(sig, filt, "fp64", engine="pocketfft")
+    out = _device(gpu, sig, filt, 0, True)
+    e, m, peak = _report(name, "fp32 half spectrum", ref, out)
+    assert e < REL_FP32
+    assert m < 1e-5 * peak
+    assert gpu.device_status() == 0
+
+
+def test_uneven_workload_real_filters_half_spectra_against_fp64(gpu, half_spectra):
+    """The 96-job batch with its real Gaussian filters passed as floats, one job at a time
+    (CONVGPU_UNEVEN_PER_JOB): jobs of 64^3 and up use half spectra."""
+    sigs, filts, _ = make_config("uneven96")
+    sizes = [s.shape[0] for s in sigs]
+    offs = np.cumsum([0] + [n ** 3 for n in sizes])
+    s = torch.from_numpy(np.concatenate([x.ravel() for x in sigs])).cuda()
+    f = torch.from_numpy(np.concatenate([x.real.astype(np.float32).ravel() for x in filts])).cuda()
+    o = torch.empty_like(s)
+    jobs = [(n, int(offs[i]), int(offs[i]), int(offs[i])) for i, n in enumerate(sizes)]
+    gpu.conv3d_uneven_device(jobs, s, f, o, gpu.NORMALIZE | gpu.FILTER_REAL | gpu.UNEVEN_PER_JOB)
+    torch.cuda.synchronize()
+    out = o.cpu().numpy()
+    refs = [conv3d(sigs[i], filts[i], "fp64", normalize=True, engine="pocketfft").ravel() for i in range(len(sizes))]
+    worst = max(rel_l2(refs[i], out[offs[i]:offs[i + 1]]) for i in range(len(sizes)))
+    e, m, peak = _report("uneven96", "fp32 half spectrum (per job)", np.concatenate(refs), out)
+    print(f"uneven96 half spectrum: worst job rel-L2 {worst:.3e}")
+    assert e < REL_FP32 and worst < REL_FP32
+    assert gpu.device_status() == 0
 
 
 @pytest.mark.parametrize("name", ["c64x1", "c128x8", "c256x4", "c512x1"])

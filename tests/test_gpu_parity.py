@@ -398,11 +398,23 @@ def _real(rng, shape):
     return rng.uniform(-1, 1, shape).astype(np.float32)
 
 
+@pytest.fixture
+def full_spectra(gpu):
+    """Real filters as full spectra (plan kind 7 = 0), whatever an earlier autotune chose."""
+    keep = {n: gpu.plan_variant(n, 7) for n in (64, 128, 256, 512)}
+    for n in keep:
+        gpu.plan_variant(n, 7, 0)
+    yield
+    for n, v in keep.items():
+        gpu.plan_variant(n, 7, v)
+
+
 @pytest.mark.parametrize("n,per_signal", [(32, False), (64, True), (128, False), (256, True)])
-def test_real_filters_device(gpu, n, per_signal):
-    """CONVGPU_FILTER_REAL on device buffers: the same result, bit for bit, as the complex
-    filter with zero imaginary parts (the real x pass uses the same radix plan and exchange
-    order), and within the reference's SNR criterion of the FP32 oracle."""
+def test_real_filters_device(gpu, full_spectra, n, per_signal):
+    """CONVGPU_FILTER_REAL on device buffers with full spectra: the same result, bit for
+    bit, as the complex filter with zero imaginary parts (the real x pass uses the same
+    radix plan and exchange order), and within the reference's SNR criterion of the FP32
+    oracle."""
     rng = np.random.default_rng(n + per_signal)
     b = 2
     sig = _c64(rng, (b, n, n, n))
@@ -424,7 +436,7 @@ def test_real_filters_device(gpu, n, per_signal):
 
 
 @pytest.mark.parametrize("per_signal", [False, True])
-def test_real_filters_host(gpu, per_signal):
+def test_real_filters_host(gpu, full_spectra, per_signal):
     """CONVGPU_FILTER_REAL through the host entry point (float filters on the host, half
     the filter upload): equal to the complex-filter call."""
     rng = np.random.default_rng(40 + per_signal)
