@@ -645,9 +645,12 @@ def run_configs(a) -> None:
         from convfpga_gb300 import build
 
         build.build()
-    rc = cg.fpga_initialize("cuda:0", "convgpu_plans.json", False)
+    replay = bool(a.plan_cache) and os.path.exists(a.plan_cache)
+    rc = cg.fpga_initialize("cuda:0", a.plan_cache or "convgpu_plans.json", False)
     if rc != 0:
         raise SystemExit(f"fpga_initialize failed: {rc} {cg.last_error()}")
+    if not replay:  # the plans of all three sizes, before anything is timed
+        cg.autotune([64, 128, 512], write_cache=bool(a.plan_cache))
     g = torch.Generator(device="cuda").manual_seed(99)
 
     def uni(shape):
@@ -662,8 +665,6 @@ def run_configs(a) -> None:
 
     results = {}
     for name, n, b in (("c64x1", 64, 1), ("c128x8", 128, 8), ("c512x1", 512, 1), ("c512x1_tc", 512, 1)):
-        if name != "c512x1_tc":
-            cg.autotune([n], write_cache=False)
         sig = uni((b, n, n, n))
         if name == "c64x1":
             filt, flags = uni((n, n, n)), cg.NORMALIZE
@@ -688,7 +689,8 @@ def run_configs(a) -> None:
         results[name] = {"conv_per_s": round(b / (ms / 1e3), 1), "ms_per_step": round(ms, 4),
                          "model_gbs": round(model / (ms / 1e3) / 1e9, 1), "steps": steps,
                          "filter": "complex U[-1,1]" if name == "c64x1" else "real Gaussian (FILTER_REAL)",
-                         "path": "tcgen05 split-TF32" if flags & cg.TENSOR_SPLIT else "plain FP32"}
+                         "path": "tcgen05 split-TF32" if flags & cg.TENSOR_SPLIT else "plain FP32",
+                         "plan": {k: cg.plan_variant(n, i) for i, k in enumerate(cg.PLAN_KINDS)}}
         del sig, filt, out
         torch.cuda.empty_cache()
     status = cg.device_status()
