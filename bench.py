@@ -546,7 +546,17 @@ def _e2e_dropin(a, cg, world, barrier) -> dict:
            "call_ms": {"min": round(1e3 * min(call_s), 3), "median": round(1e3 * statistics.median(call_s), 3),
                        "max": round(1e3 * max(call_s), 3)},
            "last_call_ms": {k: round(v, 3) for k, v in t.as_dict().items() if k != "valid"}}
-    for h in (hs, hf, ho):
+    # the same call on pinned copies of the buffers (convgpu_host_alloc), for comparison
+    ps, pf, po = (cg.PinnedBuffer.alloc(c * vol * 8) for c in (b, 1, b))
+    ps.array((b, n, n, n))[...] = sa
+    pf.array((n, n, n))[...] = fa
+    for _ in range(2):
+        assert cg.fpgaf_conv3D_svm_batch(n, ps.ptr, pf.ptr, po.ptr, b).valid, cg.last_error()
+    t0 = time.perf_counter()
+    for _ in range(calls):
+        assert cg.fpgaf_conv3D_svm_batch(n, ps.ptr, pf.ptr, po.ptr, b).valid, cg.last_error()
+    res["pinned_value"] = b * calls / (time.perf_counter() - t0)
+    for h in (hs, hf, ho, ps, pf, po):
         h.free()
     return res
 
