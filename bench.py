@@ -32,6 +32,7 @@ convolutions, no collective on the data path); value = all ranks' convolutions /
 from __future__ import annotations
 
 import argparse
+import gc
 import json
 import os
 import statistics
@@ -468,6 +469,10 @@ def _e2e(a, cg, sig, filt, shape, world, barrier, e2e_flags):
     # stall of the shared host link weighs little in the total
     e2e_steps = max(60, a.steps)
     barrier()
+    # Python's collector stays off while the calls are timed: a collection pass between two
+    # calls is host work of this script, not of the library.
+    gc.collect()
+    gc.disable()
     t0 = time.perf_counter()
     ok = True
     call_s = []
@@ -477,6 +482,7 @@ def _e2e(a, cg, sig, filt, shape, world, barrier, e2e_flags):
         call_s.append(time.perf_counter() - tc0)
         ok = ok and t.valid
     e2e_s = time.perf_counter() - t0
+    gc.enable()
     assert ok, cg.last_error()
     if world > 1:
         import torch.distributed as dist
@@ -491,7 +497,7 @@ def _e2e(a, cg, sig, filt, shape, world, barrier, e2e_flags):
            # the spread of the timed calls (the value above is their total): on a shared
            # machine a few calls can wait on the host link
            "call_ms": {"min": round(1e3 * min(call_s), 3), "median": round(1e3 * statistics.median(call_s), 3),
-                       "max": round(1e3 * max(call_s), 3)},
+                       "max": round(1e3 * max(call_s), 3), "slowest_call": call_s.index(max(call_s))},
            "last_call_ms": {k: round(v, 3) for k, v in t.as_dict().items() if k != "valid"}}
     for b in (hs, hf, ho):
         b.free()
@@ -525,6 +531,8 @@ def _e2e_dropin(a, cg, world, barrier) -> dict:
     barrier()
     call_s = []
     ok = True
+    gc.collect()
+    gc.disable()
     t0 = time.perf_counter()
     for _ in range(calls):
         tc0 = time.perf_counter()
@@ -532,6 +540,7 @@ def _e2e_dropin(a, cg, world, barrier) -> dict:
         call_s.append(time.perf_counter() - tc0)
         ok = ok and t.valid
     tot = time.perf_counter() - t0
+    gc.enable()
     assert ok, cg.last_error()
     if world > 1:
         import torch.distributed as dist
