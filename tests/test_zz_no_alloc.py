@@ -112,18 +112,20 @@ def test_no_alloc_in_place(built_lib):
 
 
 def test_no_alloc_allocates_no_device_memory(built_lib):
-    """Device free memory is the same before and after a call (the warm-up call of the
-    same size loads the kernels, which lazy module loading places in device memory)."""
+    """Device free memory is the same before and after a call. Everything else that could
+    take device memory happens before the first reading: the inputs are made (torch's own
+    kernels load lazily into device memory on their first use) and a warm-up call of the
+    same size loads this library's kernels."""
     rng = np.random.default_rng(17)
     n, b = 64, 4
     sig = torch.from_numpy(_c64(rng, (b, n, n, n))).cuda()
+    sig2 = torch.from_numpy(_c64(rng, (b, n, n, n))).cuda()
     filt = torch.from_numpy(_c64(rng, (b, n, n, n))).cuda()
     out = torch.empty_like(sig)
     cg.conv3d_device_noalloc(n, sig, filt, out, b, cg.FILTER_PER_SIGNAL)
     torch.cuda.synchronize()
     free0, _ = torch.cuda.mem_get_info()
-    sig.mul_(0.5)
-    cg.conv3d_device_noalloc(n, sig, filt, out, b, cg.FILTER_PER_SIGNAL)
+    cg.conv3d_device_noalloc(n, sig2, filt, out, b, cg.FILTER_PER_SIGNAL)
     torch.cuda.synchronize()
     free1, _ = torch.cuda.mem_get_info()
     assert free1 == free0
