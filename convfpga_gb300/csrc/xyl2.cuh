@@ -256,39 +256,16 @@ __global__ void __launch_bounds__(kXyL2Threads, 8) k_xy_l2(const __grid_constant
   const long long nitems = np * 2LL * ITEMS;
   long long ahead = 0;  // thread 0: the next item's index, claimed at this item's start
   const uint32_t spin = dep_wait_limit(status, kXyL2Spin);
-  bool ok = true;
-  // Thread 0: wait for item w's dependency (Y items) and start its tile load.
-  auto issue = [&](long long w) {
-    long long p;
-    int tl;
-    bool is_y;
-    xyl2_item<ITEMS>(w, np, lag, p, tl, is_y);
-    if (is_y) {
-      if (!wait_count(xdone + p, ITEMS, spin)) ok = false;
-      asm volatile("fence.proxy.async.global;" ::: "memory");  // generic stores -> TMA reads
-      mbar_arrive_expect_tx(bar, (uint32_t)(C * N * 8));
-      Cfg::load_y(smem_u32(tile), &mscr, tl * C, (int)(p % ring), bar);
-    } else if constexpr (TABLE) {
-      const unsigned long long q = (unsigned long long)p;
-      const CUtensorMap *m = rmaps + q / N;
-      tensormap_acquire(m);
-      mbar_arrive_expect_tx(bar, (uint32_t)(C * N * 8));
-      Cfg::load_x(smem_u32(tile), m, (int)((q % N) * N + tl * C), bar);
-    } else {
-      mbar_arrive_expect_tx(bar, (uint32_t)(C * N * 8));
-      Cfg::load_x(smem_u32(tile), &msrc, (int)(p * N + tl * C), bar);
-    }
-  };
   if (threadIdx.x == 0) {
     mbar_init(bar, 1);
     mbar_fence_init();
     *next = (long long)atomicAdd(work, 1ull);
-    if (*next < nitems) issue(*next);
   }
   for (int i = threadIdx.x; i < Cfg::TWN; i += blockDim.x) tw[i] = Cfg::tw_entry(tw512, i);
   const typename Cfg::Tw twr{tw};
   __syncthreads();
   uint32_t phase = 0;
+  bool ok = true;
   for (;;) {
     const long long w = *next;
     if (w >= nitems) break;
@@ -297,12 +274,29 @@ __global__ void __launch_bounds__(kXyL2Threads, 8) k_xy_l2(const __grid_constant
     bool is_y;
     xyl2_item<ITEMS>(w, np, lag, p, tl, is_y);
     const int slot = (int)(p % ring);
+    if (threadIdx.x == 0) {
+      if (is_y) {
+        if (!wait_count(xdone + p, ITEMS, spin)) ok = false;
+        asm volatile("fence.proxy.async.global;" ::: "memory");  // generic stores -> TMA reads
+        mbar_arrive_expect_tx(bar, (uint32_t)(C * N * 8));
+        Cfg::load_y(smem_u32(tile), &mscr, tl * C, slot, bar);
+      } else if constexpr (TABLE) {
+        const unsigned long long q = (unsigned long long)p;
+        const CUtensorMap *m = rmaps + q / N;
+        tensormap_acquire(m);
+        mbar_arrive_expect_tx(bar, (uint32_t)(C * N * 8));
+        Cfg::load_x(smem_u32(tile), m, (int)((q % N) * N + tl * C), bar);
+      } else {
+        mbar_arrive_expect_tx(bar, (uint32_t)(C * N * 8));
+        Cfg::load_x(smem_u32(tile), &msrc, (int)(p * N + tl * C), bar);
+      }
+    }
     const bool landed = __syncthreads_and(mbar_wait_bounded(bar, phase) ? 1 : 0);
     phase ^= 1u;
     if (threadIdx.x == 0) {
       if (!landed) ok = false;
       if (is_y) red_relaxed_add_u32(yread + p, 1u);  // slot read: it may be rewritten
-      ahead = (long long)atomicAdd(work, 1ull);       // loaded at the end of this item
+      ahead = (long long)atomicAdd(work, 1ull);       // published at the end of this item
     }
     float2 v[E];
     if (is_y) {
@@ -348,19 +342,15 @@ __global__ void __launch_bounds__(kXyL2Threads, 8) k_xy_l2(const __grid_constant
       float2 *o = scratch + (long long)slot * N * N + (long long)(tl * C + c) * N + t;
 #pragma unroll
       for (int e = 0; e < E; ++e) o[e * T] = v[e];
+      __syncthreads();  // every thread's stores issued
+      // The barrier orders every thread's stores before this release (cumulativity); a
+      // thread of another warp than the one issuing the loads signals it.
+      if (threadIdx.x == 32) red_release_add_u32(xdone + p, 1u);
     }
-    // this item's generic shared-memory accesses before the next item's TMA write
+    if (threadIdx.x == 0) *next = ahead;  // the atomic's latency hid behind the transform
+    // this item's generic shared-memory writes before the next item's TMA write
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    __syncthreads();  // every thread's stores issued, the tile free
-    // The X item's signal and the next item's load overlap: the release waits for this
-    // CTA's stores to be performed (cumulative over the barrier above) while thread 0
-    // starts the next tile; a thread of another warp than the one issuing the loads signals.
-    if (!is_y && threadIdx.x == 32) red_release_add_u32(xdone + p, 1u);
-    if (threadIdx.x == 0) {
-      *next = ahead;
-      if (ahead < nitems) issue(ahead);
-    }
-    __syncthreads();  // *next published
+    __syncthreads();  // *next published, tile free
   }
   if (threadIdx.x == 0 && !ok && status) atomicOr(status, kStatusQueueWait);
 }
