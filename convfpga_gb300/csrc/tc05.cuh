@@ -8,9 +8,9 @@
 //   [yr yi] = [xr xi] . [[C, -S], [S, C]]        (real form of the DFT-16 matrix)
 // in split TF32x3: x = xh + xl, M = Mh + Ml, y ~= xh.Ml + xl.Mh + xh.Mh with FP32
 // accumulation, the two small products first so that they add up at their own scale.
-// xh is x truncated to TF32 (the 13 low bits cleared), xl = x - xh (exact) truncated the
-// same way; both are exact TF32 bit patterns, made with two logical operations and one
-// packed two-lane subtraction per pair of values. One stage is P / 8 M-tiles (128 instances) x 4
+// xh is x rounded to TF32 (nearest, ties away: add half an ulp to the bit pattern, clear
+// the 13 low bits), xl = x - xh truncated to TF32; both are exact TF32 bit patterns
+// made with integer operations only. One stage is P / 8 M-tiles (128 instances) x 4
 // K-steps (K = 8 TF32) x 3 products = 12 MMAs per M-tile (kind::tf32, M = 128, N = 32) into 32 TMEM columns per
 // M-tile; each thread reads its 32 results back with tcgen05.ld.32x32b, applies the
 // FP32 twiddle W256^(n1 k2) and scatters them into the next stage's A rows.
@@ -89,18 +89,10 @@ __device__ __forceinline__ uint32_t t5_rna(float x) {
   return r;
 }
 
-// Operand split of two data values a, b at once: h = the value truncated to TF32 (its top
-// 19 bits), l = v - h (exact in FP32: it is v's low 13 mantissa bits) truncated to TF32.
-// The two subtractions are one packed two-lane instruction, so a pair costs five
-// operations. |l| < 2^-10 |v| and l loses at most 2^-10 of itself, so x = h + l holds to
-// 2^-20 |v|; the dropped product xl.Ml is below 2^-21 |x||M|.
-__device__ __forceinline__ void t5_split2(float a, float b, uint32_t &ha, uint32_t &la, uint32_t &hb,
-                                          uint32_t &lb) {
-  ha = __float_as_uint(a) & 0xFFFFE000u;
-  hb = __float_as_uint(b) & 0xFFFFE000u;
-  const float2 d = csub(make_float2(a, b), make_float2(__uint_as_float(ha), __uint_as_float(hb)));
-  la = __float_as_uint(d.x) & 0xFFFFE000u;
-  lb = __float_as_uint(d.y) & 0xFFFFE000u;
+// Operand split of a data value: (TF32 nearest of v, TF32 truncation of the rest).
+__device__ __forceinline__ uint2 t5_split(float v) {
+  const uint32_t h = (__float_as_uint(v) + 0x1000u) & 0xFFFFE000u;
+  return make_uint2(h, __float_as_uint(v - __uint_as_float(h)) & 0xFFFFE000u);
 }
 
 __device__ __forceinline__ void t5_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
@@ -147,10 +139,11 @@ __device__ __forceinline__ void t5_put_row(const T5Ctx<P> &cx, int m, const floa
   for (int kg = 0; kg < 8; ++kg) {  // one 16-byte chunk = 4 K values
     uint32_t h[4], l[4];
 #pragma unroll
-    for (int j = 0; j < 4; j += 2) {
+    for (int j = 0; j < 4; ++j) {
       const int k = kg * 4 + j;
-      t5_split2(k < 16 ? x[k].x : x[k - 16].y, k + 1 < 16 ? x[k + 1].x : x[k - 15].y, h[j], l[j], h[j + 1],
-                l[j + 1]);
+      const uint2 hl = t5_split(k < 16 ? x[k].x : x[k - 16].y);
+      h[j] = hl.x;
+      l[j] = hl.y;
     }
     const uint32_t off = t5_off(m, kg * 4);
     *reinterpret_cast<uint4 *>(cx.ah + off) = make_uint4(h[0], h[1], h[2], h[3]);
@@ -158,15 +151,11 @@ __device__ __forceinline__ void t5_put_row(const T5Ctx<P> &cx, int m, const floa
   }
 }
 
-// Writes the split parts of v.x at byte offset off_re and of v.y at off_im.
 template <int P>
-__device__ __forceinline__ void t5_put(const T5Ctx<P> &cx, uint32_t off_re, uint32_t off_im, float2 v) {
-  uint32_t hr, lr, hi, li;
-  t5_split2(v.x, v.y, hr, lr, hi, li);
-  *reinterpret_cast<uint32_t *>(cx.ah + off_re) = hr;
-  *reinterpret_cast<uint32_t *>(cx.al + off_re) = lr;
-  *reinterpret_cast<uint32_t *>(cx.ah + off_im) = hi;
-  *reinterpret_cast<uint32_t *>(cx.al + off_im) = li;
+__device__ __forceinline__ void t5_put(const T5Ctx<P> &cx, uint32_t off, float v) {
+  const uint2 hl = t5_split(v);
+  *reinterpret_cast<uint32_t *>(cx.ah + off) = hl.x;
+  *reinterpret_cast<uint32_t *>(cx.al + off) = hl.y;
 }
 
 __device__ __forceinline__ void t5_ld32(uint32_t taddr, uint32_t (&r)[32]) {
@@ -271,7 +260,8 @@ __device__ __forceinline__ void t5_fft256(T5Ctx<P> &cx, float2 (&x)[16], const f
   for (int k2 = 0; k2 < 16; ++k2) {
     const float2 v = cmul(y[k2], tw[(n1 * k2) & 255]);
     const int m2 = ROWS ? (16 * a + k2) : (P * k2 + b);
-    t5_put<P>(cx, t5_off(m2, n1), t5_off(m2, 16 + n1), v);
+    t5_put<P>(cx, t5_off(m2, n1), v.x);
+    t5_put<P>(cx, t5_off(m2, 16 + n1), v.y);
   }
   t5_mma_stage<P>(cx, x);
 }
