@@ -106,6 +106,7 @@ struct Engine {
   int device = 0;
   bool use_svm = false;
   int pageable_access = 0;
+  int pageable_host_tables = 0;  // pageable memory reached through the host's page tables
   int sm_count = 0;
   cudaStream_t sc = nullptr, sh2d = nullptr, sd2h = nullptr;
   float2 *tw512 = nullptr;
@@ -220,6 +221,7 @@ static int setup_locked(int dev, bool use_svm) {
     return -3;
   }
   cudaDeviceGetAttribute(&g.pageable_access, cudaDevAttrPageableMemoryAccess, dev);
+  cudaDeviceGetAttribute(&g.pageable_host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev);
   cudaDeviceGetAttribute(&g.sm_count, cudaDevAttrMultiProcessorCount, dev);
   int can_map = 0;
   cudaDeviceGetAttribute(&can_map, cudaDevAttrCanMapHostMemory, dev);
@@ -726,6 +728,45 @@ float ms_between(cudaEvent_t a, cudaEvent_t b) {
 }
 }  // namespace
 
+// ------------------------------------------------------------------ host copies
+// Copies between the caller's host buffers and device chunk buffers. Buffers from the
+// pinned allocator go through cudaMemcpyAsync. Pageable buffers (fpgaf_complex_malloc,
+// malloc, numpy arrays) on a device that reads pageable memory through the host's page
+// tables (GB300 over its coherent C2C link) are copied by a kernel on the copy stream: a
+// cudaMemcpyAsync from pageable memory returns only once the driver has staged the data,
+// which would serialise the pipeline's enqueue of later copies and passes, and measured
+// 176 GB/s up against 208 GB/s for a kernel reading the same pageable buffer (187 GB/s
+// for writes, the pinned figures being 211 and 193).
+__global__ void k_host_copy(const uint4 *__restrict__ src, uint4 *__restrict__ dst, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    dst[i] = src[i];
+}
+
+static bool is_pageable(const void *p) {
+  cudaPointerAttributes at{};
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeUnregistered;
+}
+
+// Kernel copies for a call whose host buffers (any of them) are pageable, where allowed.
+static bool copy_by_kernel(const void *a, const void *b, const void *c) {
+  return g.pageable_access && g.pageable_host_tables && (is_pageable(a) || is_pageable(b) || is_pageable(c));
+}
+
+static cudaError_t host_copy(void *dst, const void *src, size_t bytes, cudaMemcpyKind kind, cudaStream_t s,
+                             bool by_kernel) {
+  const bool aligned = ((reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(src) | bytes) & 15u) == 0;
+  if (!by_kernel || !aligned || bytes == 0) return cudaMemcpyAsync(dst, src, bytes, kind, s);
+  const size_t n = bytes / 16;
+  const unsigned grid = (unsigned)std::min<size_t>((n + 511) / 512, (size_t)std::max(1, g.sm_count));
+  k_host_copy<<<grid, 512, 0, s>>>(reinterpret_cast<const uint4 *>(src), reinterpret_cast<uint4 *>(dst), n);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
 // Shared-filter spectrum reuse for the host entry points (CONVGPU_FILTER_CACHED): true
 // when hfilt still holds the spectrum of this filter pointer, N and path. Any other use
 // of hfilt drops the key first; a flagged call that transforms the filter sets it again.
@@ -953,6 +994,7 @@ Timing bridge_conv_host(unsigned n, const void *sig, const void *filt, void *out
   for (unsigned b = 0; b < nbuf; ++b) freed[b] = pool.get();
 
   float2 *fspec = (float2 *)g.hfilt.p;
+  const bool kc = copy_by_kernel(sig, filt, out);  // pageable host buffers: kernel copies
   const bool half = use_half(n, real, tc);  // real filters as Hermitian half spectra
   const long long hv = half ? (long long)n * n * half_spectrum_pitch((int)n) : 0;
   const int key = tc + (real ? 8 : 0) + (half ? 16 : 0);  // path of the kept spectrum
@@ -960,7 +1002,7 @@ Timing bridge_conv_host(unsigned n, const void *sig, const void *filt, void *out
   if (!per_signal && !cached) {
     float2 *fin = real ? (float2 *)g.hreal[3].p : fspec;
     cudaEventRecord(f0, g.sh2d);
-    e = cudaMemcpyAsync(fin, filt, fbytes, cudaMemcpyHostToDevice, g.sh2d);
+    e = host_copy(fin, filt, fbytes, cudaMemcpyHostToDevice, g.sh2d, kc);
     cudaEventRecord(f1, g.sh2d);
     cudaStreamWaitEvent(g.sc, f1, 0);
     if (e == cudaSuccess)
@@ -979,8 +1021,8 @@ Timing bridge_conv_host(unsigned n, const void *sig, const void *filt, void *out
     cudaStreamWaitEvent(g.sd2h, c1[c], 0);
     cudaEventRecord(d0[c], g.sd2h);
     if (e == cudaSuccess)
-      e = cudaMemcpyAsync((float2 *)out + (size_t)first * V, g.hio[b].p, cnt * vbytes, cudaMemcpyDeviceToHost,
-                          g.sd2h);
+      e = host_copy((float2 *)out + (size_t)first * V, g.hio[b].p, cnt * vbytes, cudaMemcpyDeviceToHost, g.sd2h,
+                    kc);
     cudaEventRecord(d1[c], g.sd2h);
     cudaEventRecord(freed[b], g.sd2h);
   };
@@ -994,11 +1036,11 @@ Timing bridge_conv_host(unsigned n, const void *sig, const void *filt, void *out
     // Per-signal filters go up first: their x+y pass then runs while the signals upload.
     void *fin = real ? g.hreal[b].p : g.hfio[b].p;
     if (per_signal)
-      e = cudaMemcpyAsync(fin, (const char *)filt + (size_t)first * fbytes, cnt * fbytes, cudaMemcpyHostToDevice,
-                          g.sh2d);
+      e = host_copy(fin, (const char *)filt + (size_t)first * fbytes, cnt * fbytes, cudaMemcpyHostToDevice, g.sh2d,
+                    kc);
     cudaEventRecord(hf[c], g.sh2d);
     if (e == cudaSuccess)
-      e = cudaMemcpyAsync(io, (const float2 *)sig + (size_t)first * V, cnt * vbytes, cudaMemcpyHostToDevice, g.sh2d);
+      e = host_copy(io, (const float2 *)sig + (size_t)first * V, cnt * vbytes, cudaMemcpyHostToDevice, g.sh2d, kc);
     cudaEventRecord(h1[c], g.sh2d);
     if (e != cudaSuccess) break;
     if (c > 0) out_chunk(c - 1);

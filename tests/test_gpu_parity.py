@@ -459,3 +459,32 @@ def test_real_filters_rejected_where_unsupported(gpu):
         gpu.conv3d_device(n, s, f, s, 1, gpu.FILTER_REAL | gpu.FILTER_IS_SPECTRUM)
     with pytest.raises(gpu.ConvGpuError):
         gpu.conv3d_uneven_device([(n, 0, 0, 0)], s, f, s, gpu.FILTER_REAL)
+
+
+@pytest.mark.parametrize("offset", [0, 8])
+def test_host_pageable_and_pinned_buffers_agree(gpu, offset):
+    """The host entry point copies pageable buffers (numpy, fpgaf_complex_malloc) with a
+    kernel that reads them over the coherent link where the device allows it, and pinned
+    buffers with cudaMemcpyAsync; 8-byte aligned pageable buffers fall back to the copy
+    engines. Every route gives the same bits, and the oracle's result."""
+    rng = np.random.default_rng(91 + offset)
+    n, b = 64, 3
+    count = b * n ** 3
+    raw = np.zeros(2 * count + 2, np.complex64)  # pageable, misaligned by `offset` bytes when asked
+    sig = raw[offset // 8: offset // 8 + count].reshape(b, n, n, n)
+    sig[...] = _c64(rng, (b, n, n, n))
+    filt = _c64(rng, (n, n, n))
+    out_pageable = np.zeros_like(sig)
+    t = gpu.fpgaf_conv3D_svm_batch(n, sig, filt, out_pageable, b)
+    assert t.valid, gpu.last_error()
+    ps, pf, po = (gpu.PinnedBuffer.alloc(c * 8) for c in (count, n ** 3, count))
+    try:
+        ps.array(sig.shape)[...] = sig
+        pf.array(filt.shape)[...] = filt
+        t = gpu.fpgaf_conv3D_svm_batch(n, ps.ptr, pf.ptr, po.ptr, b)
+        assert t.valid, gpu.last_error()
+        np.testing.assert_array_equal(out_pageable, po.array(sig.shape))
+    finally:
+        for h in (ps, pf, po):
+            h.free()
+    assert snr_db(conv3d(sig, filt, "fp32"), out_pageable) > SNR_DB
