@@ -476,11 +476,14 @@ def _e2e(a, cg, sig, filt, shape, world, barrier, e2e_flags):
     t0 = time.perf_counter()
     ok = True
     call_s = []
+    slowest = None
     for _ in range(e2e_steps):
         tc0 = time.perf_counter()
         t = cg.conv3d_host(N, hs.ptr, hf.ptr, ho.ptr, BATCH, e2e_flags)
         call_s.append(time.perf_counter() - tc0)
         ok = ok and t.valid
+        if call_s[-1] == max(call_s):
+            slowest = t.as_dict()
     e2e_s = time.perf_counter() - t0
     gc.enable()
     assert ok, cg.last_error()
@@ -498,6 +501,9 @@ def _e2e(a, cg, sig, filt, shape, world, barrier, e2e_flags):
            # machine a few calls can wait on the host link
            "call_ms": {"min": round(1e3 * min(call_s), 3), "median": round(1e3 * statistics.median(call_s), 3),
                        "max": round(1e3 * max(call_s), 3), "slowest_call": call_s.index(max(call_s))},
+           # the library's own event timings of the slowest call (copies, compute): a stall
+           # outside them was on the host side of the call
+           "slowest_call_ms": {k: round(v, 3) for k, v in slowest.items() if k != "valid"},
            "last_call_ms": {k: round(v, 3) for k, v in t.as_dict().items() if k != "valid"}}
     for b in (hs, hf, ho):
         b.free()
