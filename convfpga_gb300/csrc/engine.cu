@@ -237,9 +237,18 @@ static int setup_locked(int dev, bool use_svm) {
     cudaGetLastError();
     return -4;
   }
+  // The copy streams get the highest priority: when host buffers are pageable their copies
+  // are kernels (host_copy), whose blocks are then placed ahead of pending compute blocks
+  // instead of waiting behind a persistent pass that fills the SMs. Copy-engine transfers
+  // (pinned buffers) do not depend on it.
+  int prio_low = 0, prio_high = 0;
+  if (cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high) != cudaSuccess) {
+    cudaGetLastError();
+    prio_high = 0;
+  }
   if ((e = cudaStreamCreateWithFlags(&g.sc, cudaStreamNonBlocking)) != cudaSuccess ||
-      (e = cudaStreamCreateWithFlags(&g.sh2d, cudaStreamNonBlocking)) != cudaSuccess ||
-      (e = cudaStreamCreateWithFlags(&g.sd2h, cudaStreamNonBlocking)) != cudaSuccess ||
+      (e = cudaStreamCreateWithPriority(&g.sh2d, cudaStreamNonBlocking, prio_high)) != cudaSuccess ||
+      (e = cudaStreamCreateWithPriority(&g.sd2h, cudaStreamNonBlocking, prio_high)) != cudaSuccess ||
       (e = upload_twiddles(&g.tw512)) != cudaSuccess) {
     set_err(std::string("runtime setup: ") + cudaGetErrorString(e));
     g.init = true;  // let teardown release what was created
