@@ -27,7 +27,9 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <condition_variable>
 #include <mutex>
+#include <thread>
 #include <string>
 #include <vector>
 
@@ -106,7 +108,6 @@ struct Engine {
   int device = 0;
   bool use_svm = false;
   int pageable_access = 0;
-  int pageable_host_tables = 0;  // pageable memory reached through the host's page tables
   int sm_count = 0;
   cudaStream_t sc = nullptr, sh2d = nullptr, sd2h = nullptr;
   float2 *tw512 = nullptr;
@@ -221,7 +222,6 @@ static int setup_locked(int dev, bool use_svm) {
     return -3;
   }
   cudaDeviceGetAttribute(&g.pageable_access, cudaDevAttrPageableMemoryAccess, dev);
-  cudaDeviceGetAttribute(&g.pageable_host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev);
   cudaDeviceGetAttribute(&g.sm_count, cudaDevAttrMultiProcessorCount, dev);
   int can_map = 0;
   cudaDeviceGetAttribute(&can_map, cudaDevAttrCanMapHostMemory, dev);
@@ -237,18 +237,9 @@ static int setup_locked(int dev, bool use_svm) {
     cudaGetLastError();
     return -4;
   }
-  // The copy streams get the highest priority: when host buffers are pageable their copies
-  // are kernels (host_copy), whose blocks are then placed ahead of pending compute blocks
-  // instead of waiting behind a persistent pass that fills the SMs. Copy-engine transfers
-  // (pinned buffers) do not depend on it.
-  int prio_low = 0, prio_high = 0;
-  if (cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high) != cudaSuccess) {
-    cudaGetLastError();
-    prio_high = 0;
-  }
   if ((e = cudaStreamCreateWithFlags(&g.sc, cudaStreamNonBlocking)) != cudaSuccess ||
-      (e = cudaStreamCreateWithPriority(&g.sh2d, cudaStreamNonBlocking, prio_high)) != cudaSuccess ||
-      (e = cudaStreamCreateWithPriority(&g.sd2h, cudaStreamNonBlocking, prio_high)) != cudaSuccess ||
+      (e = cudaStreamCreateWithFlags(&g.sh2d, cudaStreamNonBlocking)) != cudaSuccess ||
+      (e = cudaStreamCreateWithFlags(&g.sd2h, cudaStreamNonBlocking)) != cudaSuccess ||
       (e = upload_twiddles(&g.tw512)) != cudaSuccess) {
     set_err(std::string("runtime setup: ") + cudaGetErrorString(e));
     g.init = true;  // let teardown release what was created
@@ -738,19 +729,9 @@ float ms_between(cudaEvent_t a, cudaEvent_t b) {
 }  // namespace
 
 // ------------------------------------------------------------------ host copies
-// Copies between the caller's host buffers and device chunk buffers. Buffers from the
-// pinned allocator go through cudaMemcpyAsync. Pageable buffers (fpgaf_complex_malloc,
-// malloc, numpy arrays) on a device that reads pageable memory through the host's page
-// tables (GB300 over its coherent C2C link) are copied by a kernel on the copy stream: a
-// cudaMemcpyAsync from pageable memory returns only once the driver has staged the data,
-// which would serialise the pipeline's enqueue of later copies and passes, and measured
-// 176 GB/s up against 208 GB/s for a kernel reading the same pageable buffer (187 GB/s
-// for writes, the pinned figures being 211 and 193).
-__global__ void k_host_copy(const uint4 *__restrict__ src, uint4 *__restrict__ dst, size_t n) {
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-    dst[i] = src[i];
-}
-
+// True for pageable host memory (malloc, fpgaf_complex_malloc, numpy arrays): a
+// cudaMemcpyAsync to such memory returns only once the copy has completed (and one from it
+// once the data is staged), so the host pipeline issues its downloads from a second thread.
 static bool is_pageable(const void *p) {
   cudaPointerAttributes at{};
   if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
@@ -758,22 +739,6 @@ static bool is_pageable(const void *p) {
     return false;
   }
   return at.type == cudaMemoryTypeUnregistered;
-}
-
-// Kernel copies for a call whose host buffers (any of them) are pageable, where allowed.
-static bool copy_by_kernel(const void *a, const void *b, const void *c) {
-  return g.pageable_access && g.pageable_host_tables && (is_pageable(a) || is_pageable(b) || is_pageable(c));
-}
-
-static cudaError_t host_copy(void *dst, const void *src, size_t bytes, cudaMemcpyKind kind, cudaStream_t s,
-                             bool by_kernel) {
-  const bool aligned = ((reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(src) | bytes) & 15u) == 0;
-  if (!by_kernel || !aligned || bytes == 0) return cudaMemcpyAsync(dst, src, bytes, kind, s);
-  const size_t n = bytes / 16;
-  const unsigned grid = (unsigned)std::min<size_t>((n + 511) / 512, (size_t)std::max(1, g.sm_count));
-  k_host_copy<<<grid, 512, 0, s>>>(reinterpret_cast<const uint4 *>(src), reinterpret_cast<uint4 *>(dst), n);
-  count_launches(1);
-  return cudaGetLastError();
 }
 
 // Shared-filter spectrum reuse for the host entry points (CONVGPU_FILTER_CACHED): true
@@ -1003,7 +968,9 @@ Timing bridge_conv_host(unsigned n, const void *sig, const void *filt, void *out
   for (unsigned b = 0; b < nbuf; ++b) freed[b] = pool.get();
 
   float2 *fspec = (float2 *)g.hfilt.p;
-  const bool kc = copy_by_kernel(sig, filt, out);  // pageable host buffers: kernel copies
+  // Pageable output buffer: its downloads block the thread that issues them, so a second
+  // thread issues them (below) while this one keeps uploading and launching.
+  const bool pageable_out = is_pageable(out);
   const bool half = use_half(n, real, tc);  // real filters as Hermitian half spectra
   const long long hv = half ? (long long)n * n * half_spectrum_pitch((int)n) : 0;
   const int key = tc + (real ? 8 : 0) + (half ? 16 : 0);  // path of the kept spectrum
@@ -1011,7 +978,7 @@ Timing bridge_conv_host(unsigned n, const void *sig, const void *filt, void *out
   if (!per_signal && !cached) {
     float2 *fin = real ? (float2 *)g.hreal[3].p : fspec;
     cudaEventRecord(f0, g.sh2d);
-    e = host_copy(fin, filt, fbytes, cudaMemcpyHostToDevice, g.sh2d, kc);
+    e = cudaMemcpyAsync(fin, filt, fbytes, cudaMemcpyHostToDevice, g.sh2d);
     cudaEventRecord(f1, g.sh2d);
     cudaStreamWaitEvent(g.sc, f1, 0);
     if (e == cudaSuccess)
@@ -1023,36 +990,72 @@ Timing bridge_conv_host(unsigned n, const void *sig, const void *filt, void *out
 
   // Downloads of chunk c are enqueued after the uploads of chunk c + 1, so a download
   // waiting for its compute never sits ahead of the next upload in a copy queue.
-  auto out_chunk = [&](unsigned c) {
+  auto out_chunk = [&](unsigned c) -> cudaError_t {
     const unsigned b = c % nbuf;
     const unsigned first = c * per_chunk;
     const unsigned cnt = std::min(per_chunk, how_many - first);
     cudaStreamWaitEvent(g.sd2h, c1[c], 0);
     cudaEventRecord(d0[c], g.sd2h);
-    if (e == cudaSuccess)
-      e = host_copy((float2 *)out + (size_t)first * V, g.hio[b].p, cnt * vbytes, cudaMemcpyDeviceToHost, g.sd2h,
-                    kc);
+    const cudaError_t r = cudaMemcpyAsync((float2 *)out + (size_t)first * V, g.hio[b].p, cnt * vbytes,
+                                          cudaMemcpyDeviceToHost, g.sd2h);
     cudaEventRecord(d1[c], g.sd2h);
     cudaEventRecord(freed[b], g.sd2h);
+    return r;
   };
+  // Pageable output: a download thread takes chunk c once this thread has recorded its
+  // compute end (c1[c]); chunk buffer b is reused once the download of chunk c - nbuf has
+  // returned (which, for pageable memory, is when it has completed).
+  std::mutex dl_mu;
+  std::condition_variable dl_cv;
+  int dl_ready = -1, dl_done = -1;
+  bool dl_stop = false;
+  cudaError_t dl_err = cudaSuccess;
+  std::thread dl;
+  if (pageable_out)
+    dl = std::thread([&] {
+      for (unsigned c = 0; c < nchunks; ++c) {
+        {
+          std::unique_lock<std::mutex> lk(dl_mu);
+          dl_cv.wait(lk, [&] { return dl_stop || dl_ready >= (int)c; });
+          if (dl_ready < (int)c) return;  // stopped before chunk c was launched
+        }
+        const cudaError_t r = out_chunk(c);
+        std::lock_guard<std::mutex> lk(dl_mu);
+        if (r != cudaSuccess && dl_err == cudaSuccess) dl_err = r;
+        dl_done = (int)c;
+        dl_cv.notify_all();
+      }
+    });
   for (unsigned c = 0; c < nchunks && e == cudaSuccess; ++c) {
     const unsigned b = c % nbuf;
     const unsigned first = c * per_chunk;
     const unsigned cnt = std::min(per_chunk, how_many - first);
     float2 *io = (float2 *)g.hio[b].p;
-    if (c >= nbuf) cudaStreamWaitEvent(g.sh2d, freed[b], 0);
+    if (c >= nbuf) {
+      if (pageable_out) {
+        std::unique_lock<std::mutex> lk(dl_mu);
+        dl_cv.wait(lk, [&] { return dl_done >= (int)(c - nbuf) || dl_err != cudaSuccess; });
+        if (dl_err != cudaSuccess) {
+          e = dl_err;
+          break;
+        }
+      } else {
+        cudaStreamWaitEvent(g.sh2d, freed[b], 0);
+      }
+    }
     cudaEventRecord(h0[c], g.sh2d);
     // Per-signal filters go up first: their x+y pass then runs while the signals upload.
     void *fin = real ? g.hreal[b].p : g.hfio[b].p;
     if (per_signal)
-      e = host_copy(fin, (const char *)filt + (size_t)first * fbytes, cnt * fbytes, cudaMemcpyHostToDevice, g.sh2d,
-                    kc);
+      e = cudaMemcpyAsync(fin, (const char *)filt + (size_t)first * fbytes, cnt * fbytes, cudaMemcpyHostToDevice,
+                          g.sh2d);
     cudaEventRecord(hf[c], g.sh2d);
     if (e == cudaSuccess)
-      e = host_copy(io, (const float2 *)sig + (size_t)first * V, cnt * vbytes, cudaMemcpyHostToDevice, g.sh2d, kc);
+      e = cudaMemcpyAsync(io, (const float2 *)sig + (size_t)first * V, cnt * vbytes, cudaMemcpyHostToDevice, g.sh2d);
     cudaEventRecord(h1[c], g.sh2d);
     if (e != cudaSuccess) break;
-    if (c > 0) out_chunk(c - 1);
+    if (c > 0 && !pageable_out) e = out_chunk(c - 1);
+    if (e != cudaSuccess) break;
     cudaStreamWaitEvent(g.sc, per_signal ? hf[c] : h1[c], 0);
     cudaEventRecord(c0[c], g.sc);
     if (per_signal) {
@@ -1068,8 +1071,23 @@ Timing bridge_conv_host(unsigned n, const void *sig, const void *filt, void *out
       e = enqueue_signals(n, io, io, fspec, 0, OP_CONV, cnt, scale, g.sc, cm[c], tc, half);
     }
     cudaEventRecord(c1[c], g.sc);
+    if (pageable_out) {
+      std::lock_guard<std::mutex> lk(dl_mu);
+      dl_ready = (int)c;
+      dl_cv.notify_all();
+    }
   }
-  if (e == cudaSuccess) out_chunk(nchunks - 1);
+  if (pageable_out) {
+    {
+      std::lock_guard<std::mutex> lk(dl_mu);
+      if (e != cudaSuccess) dl_stop = true;  // chunks not launched are not downloaded
+      dl_cv.notify_all();
+    }
+    dl.join();
+    if (e == cudaSuccess) e = dl_err;
+  } else if (e == cudaSuccess) {
+    e = out_chunk(nchunks - 1);
+  }
   cudaError_t es = cudaStreamSynchronize(g.sd2h);
   cudaError_t es2 = cudaStreamSynchronize(g.sc);
   cudaError_t es3 = cudaStreamSynchronize(g.sh2d);

@@ -463,10 +463,10 @@ def test_real_filters_rejected_where_unsupported(gpu):
 
 @pytest.mark.parametrize("offset", [0, 8])
 def test_host_pageable_and_pinned_buffers_agree(gpu, offset):
-    """The host entry point copies pageable buffers (numpy, fpgaf_complex_malloc) with a
-    kernel that reads them over the coherent link where the device allows it, and pinned
-    buffers with cudaMemcpyAsync; 8-byte aligned pageable buffers fall back to the copy
-    engines. Every route gives the same bits, and the oracle's result."""
+    """The host entry point issues the downloads into a pageable output buffer (numpy,
+    fpgaf_complex_malloc) from a second thread, since such a copy returns only when it has
+    completed, and keeps pinned buffers on the calling thread. Pageable buffers (also at an
+    8-byte offset) and pinned ones give the same bits, and the oracle's result."""
     rng = np.random.default_rng(91 + offset)
     n, b = 64, 3
     count = b * n ** 3
