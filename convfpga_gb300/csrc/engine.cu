@@ -970,7 +970,7 @@ Timing bridge_conv_host(unsigned n, const void *sig, const void *filt, void *out
   float2 *fspec = (float2 *)g.hfilt.p;
   // Pageable output buffer: its downloads block the thread that issues them, so a second
   // thread issues them (below) while this one keeps uploading and launching.
-  const bool pageable_out = is_pageable(out);
+  bool pageable_out = is_pageable(out);
   const bool half = use_half(n, real, tc);  // real filters as Hermitian half spectra
   const long long hv = half ? (long long)n * n * half_spectrum_pitch((int)n) : 0;
   const int key = tc + (real ? 8 : 0) + (half ? 16 : 0);  // path of the kept spectrum
@@ -1011,21 +1011,27 @@ Timing bridge_conv_host(unsigned n, const void *sig, const void *filt, void *out
   bool dl_stop = false;
   cudaError_t dl_err = cudaSuccess;
   std::thread dl;
-  if (pageable_out)
-    dl = std::thread([&] {
-      for (unsigned c = 0; c < nchunks; ++c) {
-        {
-          std::unique_lock<std::mutex> lk(dl_mu);
-          dl_cv.wait(lk, [&] { return dl_stop || dl_ready >= (int)c; });
-          if (dl_ready < (int)c) return;  // stopped before chunk c was launched
-        }
-        const cudaError_t r = out_chunk(c);
-        std::lock_guard<std::mutex> lk(dl_mu);
-        if (r != cudaSuccess && dl_err == cudaSuccess) dl_err = r;
-        dl_done = (int)c;
-        dl_cv.notify_all();
+  auto download_loop = [&] {
+    for (unsigned c = 0; c < nchunks; ++c) {
+      {
+        std::unique_lock<std::mutex> lk(dl_mu);
+        dl_cv.wait(lk, [&] { return dl_stop || dl_ready >= (int)c; });
+        if (dl_ready < (int)c) return;  // stopped before chunk c was launched
       }
-    });
+      const cudaError_t r = out_chunk(c);
+      std::lock_guard<std::mutex> lk(dl_mu);
+      if (r != cudaSuccess && dl_err == cudaSuccess) dl_err = r;
+      dl_done = (int)c;
+      dl_cv.notify_all();
+    }
+  };
+  if (pageable_out) {
+    try {
+      dl = std::thread(download_loop);
+    } catch (...) {  // no thread to be had: downloads from this thread, as for pinned buffers
+      pageable_out = false;
+    }
+  }
   for (unsigned c = 0; c < nchunks && e == cudaSuccess; ++c) {
     const unsigned b = c % nbuf;
     const unsigned first = c * per_chunk;
