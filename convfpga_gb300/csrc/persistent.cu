@@ -301,14 +301,15 @@ __global__ void __launch_bounds__(kPThreads, 3) k_persistent_queue(const UJob *_
 // gives up sets kStatusQueueTimeout.
 // Barrier k (k = 1, 2) of a launch waits until its counter reaches k * gridDim.x; every
 // launch uses its own counter slot, zeroed before use.
-__device__ __forceinline__ bool small_grid_barrier(unsigned *slot, unsigned target, unsigned *status) {
+// spin: the probe limit, read by the caller at kernel start (dep_wait_limit) so that the
+// read stays off the barrier's critical path.
+__device__ __forceinline__ bool small_grid_barrier(unsigned *slot, unsigned target, unsigned *status, uint32_t spin) {
   __shared__ int s_ok;
   __syncthreads();  // this block's stores for the level are done
   if (threadIdx.x == 0) {
     __threadfence();  // ... and visible device-wide before the arrival
     atomicAdd(slot, 1u);
     int ok = 0;
-    const uint32_t spin = dep_wait_limit(status, kSpinLimit);
     for (uint32_t i = 0; i < spin; ++i) {
       if ((unsigned)ld_acquire(reinterpret_cast<const int *>(slot)) >= target) {
         ok = 1;
@@ -401,6 +402,7 @@ __global__ void __launch_bounds__(kPThreads, 3) k_small_conv(UJob j, unsigned *s
   extern __shared__ __align__(128) unsigned char smraw[];
   constexpr int P = small_planes_per_item<N>(), NI = N / P;  // items per cube and level
   const long long PL = (long long)P * N * N;                 // elements per item
+  const uint32_t spin = dep_wait_limit(status, kSpinLimit);
   for (int w = blockIdx.x; w < 2 * NI; w += gridDim.x) {
     if (w < NI && real)
       xy_planes_small<N, false, true>(
@@ -412,12 +414,12 @@ __global__ void __launch_bounds__(kPThreads, 3) k_small_conv(UJob j, unsigned *s
       xy_planes_small<N, false>(j.sig + (w - NI) * PL, j.out + (w - NI) * PL, 1.f, smraw, tw512);
     __syncthreads();
   }
-  if (!small_grid_barrier(slot, gridDim.x, status)) return;
+  if (!small_grid_barrier(slot, gridDim.x, status, spin)) return;
   for (int w = blockIdx.x; w < ptiles(N); w += gridDim.x) {
     run_tile<N>(j, 4, w, smraw, tw512);
     __syncthreads();
   }
-  if (!small_grid_barrier(slot, 2u * gridDim.x, status)) return;
+  if (!small_grid_barrier(slot, 2u * gridDim.x, status, spin)) return;
   for (int w = blockIdx.x; w < NI; w += gridDim.x) {
     xy_planes_small<N, true>(j.out + w * PL, j.out + w * PL, j.scale, smraw, tw512);
     __syncthreads();
