@@ -151,9 +151,11 @@ static bool capturing(cudaStream_t s) {
 
 struct CallOrder {
   cudaStream_t s;
-  bool active;
-  explicit CallOrder(cudaStream_t st) : s(st), active(!capturing(st)) {
-    if (!active || !g.last_valid || g.last_stream == s) return;
+  // Same stream as the previous call: nothing to do, not even a query (a 64^3 call is about
+  // 20 us of GPU work, so host time per call shows). Another stream: order it after the
+  // previous one unless either is being captured.
+  explicit CallOrder(cudaStream_t st) : s(st) {
+    if (!g.last_valid || g.last_stream == s || capturing(s) || capturing(g.last_stream)) return;
     if (!g.last_done && cudaEventCreateWithFlags(&g.last_done, cudaEventDisableTiming) != cudaSuccess) {
       g.last_done = nullptr;
       cudaGetLastError();
@@ -168,7 +170,6 @@ struct CallOrder {
     }
   }
   ~CallOrder() {
-    if (!active) return;
     g.last_stream = s;
     g.last_valid = true;
   }
