@@ -606,10 +606,8 @@ cudaError_t launch_small_conv(int n, const float2 *sig, const float2 *filt, floa
     grid_of[0] = grid_of[1] = grid_of[2] = 0;
     grid_dev = dev;
   }
-  // No carveout preference here (unlike the work queue): the largest shared-memory share
-  // leaves the smallest L1, and this kernel's levels are chains of L2 gathers that L1 helps
-  // (64^3: 23.2 us per convolution with it, 21.8 without); its grid of at most `widest`
-  // blocks needs one per SM.
+  // No carveout preference here (unlike the work queue): its grid of at most `widest`
+  // blocks needs one per SM, and the rest of the SM's memory can stay L1 for its gathers.
   if (grid_of[ai] == 0 &&
       (e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kPSmemBytes)) != cudaSuccess)
     return e;
