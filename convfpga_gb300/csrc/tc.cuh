@@ -127,15 +127,17 @@ struct PrecBf16x3 {
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       d[j][0] = d[j][1] = d[j][2] = d[j][3] = 0.f;
-      mma_bf16_16816(d[j], ah[0], f.h[j][0], f.h[j][1]);
-      mma_bf16_16816(d[j], ah[0], f.l[j][0], f.l[j][1]);
-      mma_bf16_16816(d[j], al[0], f.h[j][0], f.h[j][1]);
       const int jj = j ^ 2;
       const uint32_t h0 = j < 2 ? bneg(f.h[jj][0]) : f.h[jj][0], h1 = j < 2 ? bneg(f.h[jj][1]) : f.h[jj][1];
       const uint32_t l0 = j < 2 ? bneg(f.l[jj][0]) : f.l[jj][0], l1 = j < 2 ? bneg(f.l[jj][1]) : f.l[jj][1];
-      mma_bf16_16816(d[j], ah[1], h0, h1);
+      // the four small products first, so that they add up at their own scale, then the two
+      // large ones
+      mma_bf16_16816(d[j], ah[0], f.l[j][0], f.l[j][1]);
+      mma_bf16_16816(d[j], al[0], f.h[j][0], f.h[j][1]);
       mma_bf16_16816(d[j], ah[1], l0, l1);
       mma_bf16_16816(d[j], al[1], h0, h1);
+      mma_bf16_16816(d[j], ah[0], f.h[j][0], f.h[j][1]);
+      mma_bf16_16816(d[j], ah[1], h0, h1);
     }
     gather_outputs(d, y);
   }
@@ -181,20 +183,28 @@ struct PrecTf32x3 {
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       d[j][0] = d[j][1] = d[j][2] = d[j][3] = 0.f;
+      // pass 0: the small products of every k-step, so that they add up at their own
+      // scale; pass 1: the large ones
 #pragma unroll
-      for (int ks = 0; ks < 4; ++ks) {
-        const int kr = ks & 1;
-        uint32_t h0, h1, l0, l1;
-        if (ks < 2) {
-          h0 = f.h[kr][j][0], h1 = f.h[kr][j][1], l0 = f.l[kr][j][0], l1 = f.l[kr][j][1];
-        } else {
-          const int jj = j ^ 2;
-          h0 = f.h[kr][jj][0], h1 = f.h[kr][jj][1], l0 = f.l[kr][jj][0], l1 = f.l[kr][jj][1];
-          if (j < 2) h0 = fneg(h0), h1 = fneg(h1), l0 = fneg(l0), l1 = fneg(l1);
+      for (int pass = 0; pass < 2; ++pass) {
+#pragma unroll
+        for (int ks = 0; ks < 4; ++ks) {
+          const int kr = ks & 1;
+          uint32_t h0, h1, l0, l1;
+          if (ks < 2) {
+            h0 = f.h[kr][j][0], h1 = f.h[kr][j][1], l0 = f.l[kr][j][0], l1 = f.l[kr][j][1];
+          } else {
+            const int jj = j ^ 2;
+            h0 = f.h[kr][jj][0], h1 = f.h[kr][jj][1], l0 = f.l[kr][jj][0], l1 = f.l[kr][jj][1];
+            if (j < 2) h0 = fneg(h0), h1 = fneg(h1), l0 = fneg(l0), l1 = fneg(l1);
+          }
+          if (pass == 0) {
+            mma_tf32_1688(d[j], ah[ks], l0, l1);
+            mma_tf32_1688(d[j], al[ks], h0, h1);
+          } else {
+            mma_tf32_1688(d[j], ah[ks], h0, h1);
+          }
         }
-        mma_tf32_1688(d[j], ah[ks], h0, h1);
-        mma_tf32_1688(d[j], ah[ks], l0, l1);
-        mma_tf32_1688(d[j], al[ks], h0, h1);
       }
     }
     gather_outputs(d, y);
