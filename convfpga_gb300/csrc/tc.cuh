@@ -130,14 +130,14 @@ struct PrecBf16x3 {
       const int jj = j ^ 2;
       const uint32_t h0 = j < 2 ? bneg(f.h[jj][0]) : f.h[jj][0], h1 = j < 2 ? bneg(f.h[jj][1]) : f.h[jj][1];
       const uint32_t l0 = j < 2 ? bneg(f.l[jj][0]) : f.l[jj][0], l1 = j < 2 ? bneg(f.l[jj][1]) : f.l[jj][1];
-      // the four small products first, so that they add up at their own scale, then the two
-      // large ones
+      // (accumulating the small products first, as the TF32x3 paths do, measured no better
+      // here: 1.50e-5 against 1.45e-5 rel-L2; 16 significant bits per value set the error)
+      mma_bf16_16816(d[j], ah[0], f.h[j][0], f.h[j][1]);
       mma_bf16_16816(d[j], ah[0], f.l[j][0], f.l[j][1]);
       mma_bf16_16816(d[j], al[0], f.h[j][0], f.h[j][1]);
+      mma_bf16_16816(d[j], ah[1], h0, h1);
       mma_bf16_16816(d[j], ah[1], l0, l1);
       mma_bf16_16816(d[j], al[1], h0, h1);
-      mma_bf16_16816(d[j], ah[0], f.h[j][0], f.h[j][1]);
-      mma_bf16_16816(d[j], ah[1], h0, h1);
     }
     gather_outputs(d, y);
   }
