@@ -243,3 +243,22 @@ def test_tc_512_impulse_reproduces_filter(gpu):
 
 def test_tc_device_status_clean(gpu):
     assert gpu.device_status() == 0
+
+
+@pytest.mark.slow
+def test_tc_512_host_entry_point_real_filter(gpu):
+    """Config 5's shape through the host-buffer entry point: one 512^3 signal, a real filter
+    passed as floats, the tensor-core path; against the FP32 path's device result."""
+    n = 512
+    rng = np.random.default_rng(514)
+    sig = np.empty((1, n, n, n), np.complex64)
+    sig.real = rng.uniform(-1, 1, (1, n, n, n))
+    sig.imag = rng.uniform(-1, 1, (1, n, n, n))
+    filt = rng.uniform(-1, 1, (n, n, n)).astype(np.float32)
+    out = np.zeros_like(sig)
+    t = gpu.conv3d_host(n, sig, filt, out, 1, gpu.FILTER_REAL | gpu.TENSOR_SPLIT)
+    assert t.valid, gpu.last_error()
+    ref = _dev(gpu, torch.from_numpy(sig).cuda(), torch.from_numpy(filt).cuda(), 1, gpu.FILTER_REAL)
+    err = _rel_dev(ref, torch.from_numpy(out).cuda())
+    print(f"512^3 host, real filter: TC vs FP32 rel-L2 {err:.3e}")
+    assert 0.0 < err <= REL_L2_TC
