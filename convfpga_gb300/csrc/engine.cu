@@ -125,7 +125,7 @@ struct Engine {
   DevBuf hio[3];       // host API: signal chunk buffers
   DevBuf hfio[3];      // host API: per-signal filter chunk buffers
   std::string plan_path;
-  // The stream of the last call's work and an event for ordering a switch (CallOrder).
+  // End of the last call's work (CallOrder): the stream it was enqueued on and an event.
   cudaEvent_t last_done = nullptr;
   cudaStream_t last_stream = nullptr;
   bool last_valid = false;
@@ -135,11 +135,12 @@ static Engine g;
 // ------------------------------------------------------------------ cross-stream order
 // The workspace, the fused x+y pass's scratch ring and counters, and the uneven batch's
 // cached plans are shared by every call, so calls enqueued on different streams are
-// ordered on the GPU: when a call arrives on another stream than the previous call, an
-// event recorded now on the previous stream (it covers everything enqueued there so far)
-// is made a dependency of the new stream. Calls on one stream cost nothing. A stream that
-// is being captured into a graph is left alone (the graph cannot wait on work outside it):
-// a graph that contains a call must not run while another call is in flight.
+// ordered on the GPU: every call records its end on its own stream (while that stream is
+// certainly alive: a caller may destroy a stream after its last call), and a call on
+// another stream than the previous one first makes that event a dependency of its stream.
+// A stream that is being captured into a graph is left alone (the graph cannot wait on
+// work outside it): a graph that contains a call must not run while another call is in
+// flight.
 static bool capturing(cudaStream_t s) {
   cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
   if (cudaStreamIsCapturing(s, &st) != cudaSuccess) {
@@ -151,27 +152,24 @@ static bool capturing(cudaStream_t s) {
 
 struct CallOrder {
   cudaStream_t s;
-  // Same stream as the previous call: nothing to do, not even a query (a 64^3 call is about
-  // 20 us of GPU work, so host time per call shows). Another stream: order it after the
-  // previous one unless either is being captured.
-  explicit CallOrder(cudaStream_t st) : s(st) {
-    if (!g.last_valid || g.last_stream == s || capturing(s) || capturing(g.last_stream)) return;
+  bool active;
+  explicit CallOrder(cudaStream_t st) : s(st), active(!capturing(st)) {
+    if (active && g.last_valid && g.last_stream != s) cudaStreamWaitEvent(s, g.last_done, 0);
+  }
+  // Records even when the call failed partway: the event then follows what was enqueued.
+  ~CallOrder() {
+    if (!active) return;
     if (!g.last_done && cudaEventCreateWithFlags(&g.last_done, cudaEventDisableTiming) != cudaSuccess) {
       g.last_done = nullptr;
       cudaGetLastError();
-      cudaDeviceSynchronize();  // no event to be had: wait for everything instead
       return;
     }
-    if (cudaEventRecord(g.last_done, g.last_stream) == cudaSuccess) {
-      cudaStreamWaitEvent(s, g.last_done, 0);
-    } else {  // the previous stream is gone: its work is still ordered by a device-wide wait
+    if (cudaEventRecord(g.last_done, s) == cudaSuccess) {
+      g.last_stream = s;
+      g.last_valid = true;
+    } else {
       cudaGetLastError();
-      cudaDeviceSynchronize();
     }
-  }
-  ~CallOrder() {
-    g.last_stream = s;
-    g.last_valid = true;
   }
 };
 
