@@ -47,7 +47,9 @@ extern "C" {
  * Tensor-core path: the radix-16 stages of N = 256 transforms run as 16-point DFT
  * matmuls on the tensor cores with split operands and FP32 accumulation (TF32x3:
  * ~1e-7 relative error per 256-point transform; BF16x3: ~4e-6, which exceeds 1e-5
- * relative L2 end to end on 256^3 convolutions). Other N run the FP32 kernels.
+ * relative L2 end to end on 256^3 convolutions). N = 512 with TF32x3 runs a radix-2
+ * step on the CUDA cores around two such 256-point transforms. Other N, and BF16x3 at
+ * N = 512, run the FP32 kernels.
  * Real filters (CONVGPU_FILTER_REAL): d_filter holds N^3 floats per filter cube (4-byte
  * aligned); the filter's first pass reads them directly, half the bytes of a complex
  * filter, and the result equals that of the same filter given as complex values with
