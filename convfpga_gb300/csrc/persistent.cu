@@ -166,8 +166,12 @@ __device__ __noinline__ void run_tile(const UJob &j, int pass, int tile, unsigne
     if (op == OP_INV) swap_all(v);
     fft_forward<N, E>(v, t, tw, buf, sidx, typename S::Plan{});
     if (op == OP_INV) swap_all(v);
+    if (scale != 1.0f) {
 #pragma unroll
-    for (int e = 0; e < E; ++e) dst[(row0 + c) * N + t + e * T] = make_float2(v[e].x * scale, v[e].y * scale);
+      for (int e = 0; e < E; ++e) v[e] = make_float2(v[e].x * scale, v[e].y * scale);
+    }
+#pragma unroll
+    for (int e = 0; e < E; ++e) dst[(row0 + c) * N + t + e * T] = v[e];
     return;
   }
   // Strided pencils pid = tile*COLS + c; slot (n, c) = n*COLS + c.
@@ -382,8 +386,12 @@ __device__ __noinline__ void xy_planes_small(const float2 *src, float2 *dst, flo
     if (INV) swap_all(v);
     fft_forward<N, E>(v, t, tw, pl, sidx, typename S::Plan{});
     if (INV) swap_all(v);
+    if (scale != 1.0f) {
 #pragma unroll
-    for (int e = 0; e < E; ++e) dst[sidx(t + e * T)] = make_float2(v[e].x * scale, v[e].y * scale);
+      for (int e = 0; e < E; ++e) v[e] = make_float2(v[e].x * scale, v[e].y * scale);
+    }
+#pragma unroll
+    for (int e = 0; e < E; ++e) dst[sidx(t + e * T)] = v[e];
     __syncthreads();  // this round's columns read back before the next round's exchange
   }
 }

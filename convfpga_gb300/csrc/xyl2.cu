@@ -126,7 +126,7 @@ static cudaError_t launch_common(const CUtensorMap *msrc_or_null, const CUtensor
   const long long items = 2LL * nplanes * (N / Cfg::C);
   const unsigned grid = (unsigned)std::min<long long>(items, (long long)ps * sms);
   kern<<<grid, kXyL2Threads, xyl2_smem<N>(), s>>>(msrc, mscr, reinterpret_cast<float2 *>(ring->p), dst, nplanes,
-                                                   scale, tw512, ctr, status, Cfg::LAG, Cfg::RING, rmaps, dsts);
+                                                   scale, tw512, ctr, status, Cfg::LAG, rmaps, dsts);
   return cudaGetLastError();
 }
 
@@ -193,7 +193,7 @@ cudaError_t launch_xy_l2_tc(const float2 *src, float2 *dst, int nplanes, bool in
   const unsigned grid = (unsigned)std::min<long long>(items, (long long)per_sm * sms);
   auto kern = inverse ? k_xy_l2_tc<true> : k_xy_l2_tc<false>;
   kern<<<grid, kXyTcThreads, kXyTcSmem, s>>>(msrc, mscr, reinterpret_cast<float2 *>(ring->p), dst, nplanes, scale,
-                                             tw512, ctr, status, Cfg::LAG, Cfg::RING);
+                                             tw512, ctr, status, Cfg::LAG);
   return cudaGetLastError();
 }
 

@@ -228,7 +228,7 @@ constexpr int xyl2_smem() {
   return 128 + XyL2Cfg<N>::C * N * 8 + XyL2Cfg<N>::TWN * 8 + 16;
 }
 
-// msrc: 2D map over the source rows (box {N, C}); mscr: 3D map over the `ring` scratch
+// msrc: 2D map over the source rows (box {N, C}); mscr: 3D map over the Cfg::RING scratch
 // planes (box {C, N, 1}). ctr: 2 * np counters (X stores done, Y reads done) and the
 // work counter at ctr[2 * np], all zero at launch.
 // TABLE: the planes belong to np / N cubes at unrelated addresses; plane p is plane p % N
@@ -239,10 +239,10 @@ __global__ void __launch_bounds__(kXyL2Threads, 8) k_xy_l2(const __grid_constant
                                                            const __grid_constant__ CUtensorMap mscr, float2 *scratch,
                                                            float2 *dst, long long np, float scale,
                                                            const float2 *tw512, unsigned *ctr, unsigned *status,
-                                                           int lag_planes, int ring, const CUtensorMap *rmaps,
+                                                           int lag_planes, const CUtensorMap *rmaps,
                                                            float2 *const *dsts) {
   using Cfg = XyL2Cfg<N>;
-  constexpr int E = 16, T = N / E, C = Cfg::C, ITEMS = N / C;
+  constexpr int E = 16, T = N / E, C = Cfg::C, ITEMS = N / C, RING = Cfg::RING;
   static_assert(C * T == kXyL2Threads, "an item is one pencil tile per thread group");
   using Plan = typename Cfg::Plan;
   extern __shared__ __align__(128) unsigned char smraw[];
@@ -273,7 +273,7 @@ __global__ void __launch_bounds__(kXyL2Threads, 8) k_xy_l2(const __grid_constant
     int tl;
     bool is_y;
     xyl2_item<ITEMS>(w, np, lag, p, tl, is_y);
-    const int slot = (int)(p % ring);
+    const int slot = (int)((unsigned)p % (unsigned)RING);  // p < np < 2^31: a 32-bit remainder by a constant
     if (threadIdx.x == 0) {
       if (is_y) {
         if (!wait_count(xdone + p, ITEMS, spin)) ok = false;
@@ -331,12 +331,16 @@ __global__ void __launch_bounds__(kXyL2Threads, 8) k_xy_l2(const __grid_constant
       } else {
         o = dst + p * N * N + tl * C + c;
       }
+      if (scale != 1.0f) {  // the same value for every item: a uniform branch
 #pragma unroll
-      for (int e = 0; e < E; ++e) o[(long long)(t + e * T) * N] = make_float2(v[e].x * scale, v[e].y * scale);
+        for (int e = 0; e < E; ++e) v[e] = make_float2(v[e].x * scale, v[e].y * scale);
+      }
+#pragma unroll
+      for (int e = 0; e < E; ++e) o[(long long)(t + e * T) * N] = v[e];
     } else {
       const int t = threadIdx.x % T, c = threadIdx.x / T;
-      if (p >= ring) {  // the slot's previous plane must have been read
-        if (threadIdx.x == 0 && !wait_count(yread + (p - ring), ITEMS, spin)) ok = false;
+      if (p >= RING) {  // the slot's previous plane must have been read
+        if (threadIdx.x == 0 && !wait_count(yread + (p - RING), ITEMS, spin)) ok = false;
         __syncthreads();
       }
       float2 *o = scratch + (long long)slot * N * N + (long long)(tl * C + c) * N + t;

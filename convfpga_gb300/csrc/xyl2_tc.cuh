@@ -32,8 +32,8 @@ template <bool INV>
 __global__ void __launch_bounds__(kXyTcThreads, kXyTcMinBlocks)
     k_xy_l2_tc(const __grid_constant__ CUtensorMap msrc, const __grid_constant__ CUtensorMap mscr, float2 *scratch,
                float2 *dst, long long np, float scale, const float2 *tw512, unsigned *ctr, unsigned *status,
-               int lag_planes, int ring) {
-  constexpr int N = 256, C = 8, ITEMS = N / C, TILE = N * C;
+               int lag_planes) {
+  constexpr int N = 256, C = 8, ITEMS = N / C, TILE = N * C, RING = XyL2Cfg<256>::RING;
   using G = T5Geom<8>;
   static_assert(TILE * 8 == G::kABytes, "a tile is one A operand part");
   constexpr uint32_t kCols = 32;
@@ -96,7 +96,7 @@ __global__ void __launch_bounds__(kXyTcThreads, kXyTcMinBlocks)
     int tl;
     bool is_y;
     xyl2_item<ITEMS>(w, np, lag, p, tl, is_y);
-    const int slot = (int)(p % ring);
+    const int slot = (int)((unsigned)p % (unsigned)RING);  // p < np < 2^31
     if (threadIdx.x == 0) {
       if (is_y) {
         if (!wait_count(xdone + p, ITEMS, spin)) ok = false;
@@ -137,11 +137,15 @@ __global__ void __launch_bounds__(kXyTcThreads, kXyTcMinBlocks)
     }
     if (is_y) {
       float2 *o = dst + p * N * N + tl * C + ib;
+      if (scale != 1.0f) {
 #pragma unroll
-      for (int k = 0; k < 16; ++k) o[(long long)(ia + 16 * k) * N] = make_float2(v[k].x * scale, v[k].y * scale);
+        for (int k = 0; k < 16; ++k) v[k] = make_float2(v[k].x * scale, v[k].y * scale);
+      }
+#pragma unroll
+      for (int k = 0; k < 16; ++k) o[(long long)(ia + 16 * k) * N] = v[k];
     } else {
-      if (p >= ring) {  // the slot's previous plane must have been read
-        if (threadIdx.x == 0 && !wait_count(yread + (p - ring), ITEMS, spin)) ok = false;
+      if (p >= RING) {  // the slot's previous plane must have been read
+        if (threadIdx.x == 0 && !wait_count(yread + (p - RING), ITEMS, spin)) ok = false;
         __syncthreads();
       }
       float2 *o = scratch + (long long)slot * N * N + (long long)(tl * C + ia) * N + ib;
