@@ -68,10 +68,11 @@ def test_sizes_against_fp32_oracle(gpu, n, per_signal):
 
 @pytest.mark.parametrize("n", [32, 256])
 @pytest.mark.parametrize("how_many", [1, 2, 3])
-def test_shared_filter_batches_against_fp32_oracle(gpu, n, how_many):
+def test_shared_filter_batches_against_fp32_oracle(gpu, full_spectra, n, how_many):
     """A shared filter with one or two signals has its z transform fused into the signals'
     z pass; from three signals on it gets a pass of its own. Both routes, complex and real
-    filters (the real one bit-identical to the same filter given as complex)."""
+    filters (the real one, as a full spectrum, bit-identical to the same filter given as
+    complex)."""
     rng = np.random.default_rng(100 * how_many + n)
     sig = _c64(rng, (how_many, n, n, n))
     filt = _c64(rng, (n, n, n))

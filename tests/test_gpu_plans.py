@@ -26,10 +26,12 @@ def _c64(rng, shape):
 
 @pytest.fixture
 def restore_plans(gpu):
+    """Puts every plan kind of every size back as it was: the autotuner below also sets the
+    tensor-core and half-spectrum kinds, which later tests in the session rely on."""
+    keep = {(n, k): gpu.plan_variant(n, k) for n in (16, 32, 64, 128, 256, 512) for k in range(len(gpu.PLAN_KINDS))}
     yield
-    for n in (16, 32, 64, 128, 256, 512):
-        for k in range(KINDS + 1):
-            gpu.plan_variant(n, k, 0)
+    for (n, k), v in keep.items():
+        gpu.plan_variant(n, k, v)
 
 
 def _check(gpu, n, b, per_signal):
