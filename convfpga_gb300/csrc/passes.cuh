@@ -262,7 +262,10 @@ __global__ void __launch_bounds__(COLS *(N / E)) k_strided_tma(const __grid_cons
   float2 *tile = reinterpret_cast<float2 *>(smraw + 128);
   float2 *ftile = tile + TILE;
   float2 *tw = HAS_F ? ftile + TILE : tile + TILE;
-  const uint32_t bar = smem_u32(smraw);
+  // bar: the signal tile; fbar: the filter tile. CONV_FZ issues the filter first and
+  // transforms it while the signal lands; CONV needs the filter only for the product, so
+  // it lands during the signal's transform.
+  const uint32_t bar = smem_u32(smraw), fbar = bar + 8;
 
   const int vol = blockIdx.x / a.groups_per_vol;
   const int r = blockIdx.x % a.groups_per_vol;
@@ -271,39 +274,52 @@ __global__ void __launch_bounds__(COLS *(N / E)) k_strided_tma(const __grid_cons
 
   if (threadIdx.x == 0) {
     mbar_init(bar, 1);
+    if constexpr (HAS_F) mbar_init(fbar, 1);
     mbar_fence_init();
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    const CUtensorMap *ms = a.maps ? a.maps + vol : &msrc;
-    const int zoff = a.maps ? 0 : vol * N;
-    if (a.maps) tensormap_acquire(ms);
-    mbar_arrive_expect_tx(bar, (HAS_F ? 2u : 1u) * TILE * 8u);
+    auto load_signal = [&]() {
+      const CUtensorMap *ms = a.maps ? a.maps + vol : &msrc;
+      const int zoff = a.maps ? 0 : vol * N;
+      if (a.maps) tensormap_acquire(ms);
+      mbar_arrive_expect_tx(bar, TILE * 8u);
 #pragma unroll
-    for (int l = 0; l < NLOADS; ++l) {
-      if (axis == 1)
-        tma_load_3d(smem_u32(tile + l * NBOX * COLS), ms, x0, l * NBOX, zoff + row, bar);
-      else
-        tma_load_3d(smem_u32(tile + l * NBOX * COLS), ms, x0, row, zoff + l * NBOX, bar);
-      if constexpr (HAS_F) {
-        const CUtensorMap *mf = a.fmaps ? a.fmaps + vol : &mfilt;
-        const int fzoff = a.fmaps ? 0 : (a.filt_vol_elems ? vol : 0) * N;
-        if (a.fmaps && l == 0) tensormap_acquire(mf);
-        tma_load_3d(smem_u32(ftile + l * NBOX * COLS), mf, x0, row, fzoff + l * NBOX, bar);
+      for (int l = 0; l < NLOADS; ++l) {
+        if (axis == 1)
+          tma_load_3d(smem_u32(tile + l * NBOX * COLS), ms, x0, l * NBOX, zoff + row, bar);
+        else
+          tma_load_3d(smem_u32(tile + l * NBOX * COLS), ms, x0, row, zoff + l * NBOX, bar);
       }
-    }
+    };
+    auto load_filter = [&]() {
+      const CUtensorMap *mf = a.fmaps ? a.fmaps + vol : &mfilt;
+      const int fzoff = a.fmaps ? 0 : (a.filt_vol_elems ? vol : 0) * N;
+      if (a.fmaps) tensormap_acquire(mf);
+      mbar_arrive_expect_tx(fbar, TILE * 8u);
+#pragma unroll
+      for (int l = 0; l < NLOADS; ++l)
+        tma_load_3d(smem_u32(ftile + l * NBOX * COLS), mf, x0, row, fzoff + l * NBOX, fbar);
+    };
+    if constexpr (OP == OP_CONV_FZ) load_filter();
+    load_signal();
+    if constexpr (OP == OP_CONV) load_filter();
   }
   for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = a.tw512[i * (512 / N)];
   const int c = threadIdx.x % COLS;
   const int t = threadIdx.x / COLS;
   const ColSlot<COLS> sidx{c};
-  // Uniform decision: every thread takes the same branch, so no barrier is left waiting.
-  const int ok = __syncthreads_and(mbar_wait_bounded(bar, 0) ? 1 : 0);
-  if (!ok) {
+  // Each wait is a uniform decision (every thread takes the same branch, so no barrier is
+  // left waiting); one that gives up lets the copies still in flight land before the CTA
+  // exits.
+  auto landed = [&](uint32_t b) {
+    if (__syncthreads_and(mbar_wait_bounded(b, 0) ? 1 : 0)) return true;
     if (threadIdx.x == 0 && a.status) atomicOr(a.status, kStatusTmaTimeout);
-    mbar_wait_bounded(bar, 0);  // let copies still in flight land before the CTA exits
-    return;
-  }
+    mbar_wait_bounded(bar, 0);
+    if constexpr (HAS_F) mbar_wait_bounded(fbar, 0);
+    return false;
+  };
+  if (!landed(OP == OP_CONV_FZ ? fbar : bar)) return;
 
   float2 v[E];
   if constexpr (OP == OP_CONV_FZ) {
@@ -314,6 +330,7 @@ __global__ void __launch_bounds__(COLS *(N / E)) k_strided_tma(const __grid_cons
     fft_forward<N, E>(f, t, tw, ftile, sidx, Plan{});
 #pragma unroll
     for (int e = 0; e < E; ++e) ftile[sidx(t + e * T)] = f[e];  // own slots: read back by this thread only
+    if (!landed(bar)) return;
   }
 #pragma unroll
   for (int e = 0; e < E; ++e) v[e] = tile[sidx(t + e * T)];
@@ -327,6 +344,9 @@ __global__ void __launch_bounds__(COLS *(N / E)) k_strided_tma(const __grid_cons
     swap_all(v);
   } else {
     fft_forward<N, E>(v, t, tw, tile, sidx, Plan{});
+    if constexpr (OP == OP_CONV) {
+      if (!landed(fbar)) return;
+    }
 #pragma unroll
     for (int e = 0; e < E; ++e) v[e] = cmul(v[e], ftile[sidx(t + e * T)]);
     swap_all(v);
