@@ -34,8 +34,15 @@ constexpr int zconv_half_smem_bytes() {
   return 128 + (2 * N * COLS + N * (COLS + 2)) * 8 + N * 8;
 }
 
+// CTAs per SM that shared memory allows (26 KB at N = 64, about 52 KB at 128 and 256,
+// 111 KB at 512): registers are held to that occupancy too.
+template <int N>
+constexpr int zconv_half_min_blocks() {
+  return N <= 64 ? 8 : (N <= 256 ? 4 : 2);
+}
+
 template <int N, int E, int COLS, class Plan>
-__global__ void __launch_bounds__(2 * COLS *(N / E)) k_zconv_half(const __grid_constant__ CUtensorMap msig,
+__global__ void __launch_bounds__(2 * COLS *(N / E), zconv_half_min_blocks<N>()) k_zconv_half(const __grid_constant__ CUtensorMap msig,
                                                                  const __grid_constant__ CUtensorMap mhalf,
                                                                  PassArgs a) {
   constexpr int T = N / E, TILE = N * COLS, FC = COLS + 2;
@@ -45,7 +52,7 @@ __global__ void __launch_bounds__(2 * COLS *(N / E)) k_zconv_half(const __grid_c
   float2 *tiles = reinterpret_cast<float2 *>(smraw + 128);  // A, then B
   float2 *ftile = tiles + 2 * TILE;                          // [kz][C + 2]
   float2 *tw = ftile + N * FC;
-  const uint32_t bar = smem_u32(smraw);
+  const uint32_t bar = smem_u32(smraw), fbar = bar + 8;  // the two signal tiles; the filter tile
 
   const int vol = blockIdx.x / (N * GROUPS);
   const int r = blockIdx.x % (N * GROUPS);
@@ -54,18 +61,23 @@ __global__ void __launch_bounds__(2 * COLS *(N / E)) k_zconv_half(const __grid_c
 
   if (threadIdx.x == 0) {
     mbar_init(bar, 1);
+    mbar_init(fbar, 1);
     mbar_fence_init();
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    mbar_arrive_expect_tx(bar, (uint32_t)((2 * TILE + N * FC) * 8));
-    const int fz = (a.filt_vol_elems ? vol : 0) * N;
+    // the signal tiles first: the filter tile is needed only for the product, after their
+    // transforms
+    mbar_arrive_expect_tx(bar, (uint32_t)(2 * TILE * 8));
 #pragma unroll
     for (int l = 0; l < NLOADS; ++l) {
       tma_load_3d(smem_u32(tiles + l * NBOX * COLS), &msig, x0, y, vol * N + l * NBOX, bar);
       tma_load_3d(smem_u32(tiles + TILE + l * NBOX * COLS), &msig, xb, yb, vol * N + l * NBOX, bar);
-      tma_load_3d(smem_u32(ftile + l * NBOX * FC), &mhalf, x0, y, fz + l * NBOX, bar);
     }
+    mbar_arrive_expect_tx(fbar, (uint32_t)(N * FC * 8));
+    const int fz = (a.filt_vol_elems ? vol : 0) * N;
+#pragma unroll
+    for (int l = 0; l < NLOADS; ++l) tma_load_3d(smem_u32(ftile + l * NBOX * FC), &mhalf, x0, y, fz + l * NBOX, fbar);
   }
   for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = a.tw512[i * (512 / N)];
   const int g = threadIdx.x / (COLS * T);  // 0: tile A, 1: tile B
@@ -73,17 +85,22 @@ __global__ void __launch_bounds__(2 * COLS *(N / E)) k_zconv_half(const __grid_c
   const int c = local % COLS, t = local / COLS;
   float2 *tile = tiles + g * TILE;
   const ColSlot<COLS> sidx{c};
-  const int ok = __syncthreads_and(mbar_wait_bounded(bar, 0) ? 1 : 0);
-  if (!ok) {
+  // Each wait is a uniform decision; one that gives up lets the copies still in flight
+  // land before the CTA exits.
+  auto landed = [&](uint32_t b) {
+    if (__syncthreads_and(mbar_wait_bounded(b, 0) ? 1 : 0)) return true;
     if (threadIdx.x == 0 && a.status) atomicOr(a.status, kStatusTmaTimeout);
-    mbar_wait_bounded(bar, 0);  // let copies still in flight land before the CTA exits
-    return;
-  }
+    mbar_wait_bounded(bar, 0);
+    mbar_wait_bounded(fbar, 0);
+    return false;
+  };
+  if (!landed(bar)) return;
   float2 v[E];
 #pragma unroll
   for (int e = 0; e < E; ++e) v[e] = tile[sidx(t + e * T)];
   __syncthreads();
   fft_forward<N, E>(v, t, tw, tile, sidx, Plan{});
+  if (!landed(fbar)) return;
 #pragma unroll
   for (int e = 0; e < E; ++e) {
     const int kz = t + e * T;
