@@ -25,6 +25,8 @@ roofline   : the dominant pass kernel: algorithmic bytes per launch / mean launc
 cpu_baseline: the CPU FFT convolution (pocketfft complex64, all host threads; FFTW3 is not
              installed) on a bounded sample, rank 0 at N=1 only.
 --impl reference: times that CPU implementation alone as the reference arm.
+--workload configs / uneven96: the other single-GPU workloads; each line carries a
+             cpu_baseline of its own (the same pipeline over the same jobs on the host cores).
 
 Multi-GPU (torchrun, one rank per GPU): every rank convolves its own batch of 4 (independent
 convolutions, no collective on the data path); value = all ranks' convolutions / max time.
@@ -227,6 +229,68 @@ def cpu_baseline(budget_s: float = 20.0) -> dict:
             "sample": f"median of {len(ts)} single 256^3 convolutions (filter FFT + signal FFT + multiply + "
                       f"inverse FFT, pocketfft complex64, {workers} threads; FFTW3 unavailable - pocketfft "
                       f"stand-in), one of the 4 per step"}
+
+
+def _cpu_jobs_seconds(jobs, workers: int) -> float:
+    """Seconds for the CPU path over `jobs` = [(n, signals, filter per signal)]: one
+    forward FFT per distinct filter, then per signal its FFT, the product and the inverse
+    FFT (src/fft_conv3D.cpp:50-177), pocketfft complex64. Inputs are U[-1,1] complex64: the
+    timing of an FFT does not depend on the values."""
+    import numpy as np
+    import scipy.fft as sfft
+
+    from oracle import comp_mult
+
+    rng = np.random.default_rng(11)
+    tot = 0.0
+    for n, count, per_signal in jobs:
+        a = rng.uniform(-1, 1, (2, n, n, n)).astype(np.float32)
+        x = (a[0] + 1j * a[1]).astype(np.complex64)
+        del a
+        t0 = time.perf_counter()
+        fs = None
+        for _ in range(count):
+            if fs is None or per_signal:
+                fs = sfft.fftn(x, workers=workers)
+            ss = sfft.fftn(x, workers=workers)
+            sfft.ifftn(comp_mult(ss, fs), norm="forward", workers=workers)
+        tot += time.perf_counter() - t0
+    return tot
+
+
+def cpu_configs_baseline(names, budget_s: float = 8.0) -> dict:
+    """CPU conv/s of each single-GPU workload on all host threads: 64^3 x1 and 128^3 x8 as
+    whole steps (median of up to 5), 512^3 x1 as a slice of one convolution (the same
+    transforms on m/512 of the planes and columns, about three seconds) scaled up."""
+    workers = os.cpu_count() or 1
+    out = {}
+    for name in names:
+        n, b = {"c64x1": (64, 1), "c128x8": (128, 8), "c512x1": (512, 1)}[name]
+        if n <= 256:
+            _cpu_jobs_seconds([(n, 1, False)], workers)  # warm-up (plans, page faults)
+            t1 = _cpu_jobs_seconds([(n, b, False)], workers)
+            reps = max(1, min(5, int(budget_s / max(t1, 1e-3))))
+            ts = [t1] + [_cpu_jobs_seconds([(n, b, False)], workers) for _ in range(reps - 1)]
+            value = b / statistics.median(ts)
+            sample = f"median of {len(ts)} steps of {b} {n}^3 convolution(s) with one shared filter"
+        else:
+            import numpy as np
+
+            rng = np.random.default_rng(12)
+            sig = np.empty((n, n, n), np.complex64)
+            sig.real = rng.uniform(-1, 1, (n, n, n)).astype(np.float32)
+            sig.imag = 0.0
+            filt = sig.copy()
+            t = _cpu_conv_sample(1.0 / 64, sig, filt, workers)  # 1/64 of a convolution
+            m = max(1, min(n, int(round(n * 3.0 / max(64 * t, 1e-3)))))  # a slice of about 3 s
+            t = _cpu_conv_sample(m / n, sig, filt, workers)
+            value = (m / n) / t
+            sample = f"{m}/{n} of one {n}^3 convolution (filter FFT + signal FFT + multiply + inverse FFT), scaled"
+            del sig, filt
+        out[name] = {"value": round(value, 3), "unit": "conv/s", "cores": workers, "kind": "port",
+                     "sample": sample + f", pocketfft complex64, {workers} threads (FFTW3 unavailable - "
+                                        "pocketfft stand-in)"}
+    return {"cpu_model": _cpu_model(), "configs": out}
 
 
 def run_reference(a) -> None:
@@ -651,6 +715,15 @@ def run_uneven(a) -> None:
         "plan": {str(n): {k: cg.plan_variant(n, i) for i, k in enumerate(cg.PLAN_KINDS)} for n in sorted(set(sizes))},
         "gpu_launches": launches_g, "device_status": status, "clocks": clocks,
     }
+    if not a.no_cpu_baseline:  # the same 96 convolutions on the host cores
+        workers = os.cpu_count() or 1
+        _cpu_jobs_seconds([(n, 1, True) for n in sorted(set(sizes))], workers)  # warm-up
+        t = _cpu_jobs_seconds([(n, 1, True) for n in sizes], workers)
+        line["cpu_baseline"] = {"value": round(len(sizes) / t, 3), "unit": "conv/s", "cores": workers, "kind": "port",
+                                "cpu_model": _cpu_model(),
+                                "sample": f"one pass over the 96 convolutions, each with its own filter "
+                                          f"(filter FFT + signal FFT + multiply + inverse FFT), pocketfft "
+                                          f"complex64, {workers} threads (FFTW3 unavailable - pocketfft stand-in)"}
     print(json.dumps(line), flush=True)
 
 
@@ -724,6 +797,8 @@ def run_configs(a) -> None:
             "warmup": a.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded torch generator)", "config": {"workload": "configs", "value_of": "c128x8"},
             "configs": results, "device_status": status}
+    if not a.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_configs_baseline(["c64x1", "c128x8", "c512x1"])
     print(json.dumps(line), flush=True)
 
 

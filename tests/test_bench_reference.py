@@ -28,3 +28,17 @@ def test_reference_arm_prints_one_contract_line():
     assert line["e2e"] == {"value": line["value"], "unit": "conv/s", "h2d_bytes_per_step": 0,
                            "d2h_bytes_per_step": 0}
     assert "workload" in line["config"]
+
+
+def test_cpu_baselines_of_the_other_workloads():
+    """The CPU rates that `--workload configs` and `--workload uneven96` report beside their
+    GPU numbers: the same pipeline over the same job list (small sizes here)."""
+    sys.path.insert(0, ROOT)
+    import bench
+
+    t = bench._cpu_jobs_seconds([(16, 2, False), (32, 1, True)], 2)
+    assert t > 0
+    r = bench.cpu_configs_baseline(["c64x1"], budget_s=0.5)
+    c = r["configs"]["c64x1"]
+    assert r["cpu_model"] and c["value"] > 0 and c["unit"] == "conv/s" and c["kind"] == "port"
+    assert c["cores"] >= 1 and "pocketfft" in c["sample"]
