@@ -116,12 +116,6 @@ static __global__ void k_tc05_consts(unsigned char *blk, const float2 *tw512) {
   for (int i = threadIdx.x; i < 256; i += blockDim.x) tw[i] = tw512[2 * i];
 }
 
-__device__ __forceinline__ void bulk_load(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar) {
-  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
-               "l"(reinterpret_cast<uint64_t>(src)), "r"(bytes), "r"(bar)
-               : "memory");
-}
-
 template <int P>
 struct T5Ctx {
   unsigned char *ah, *al;  // A operand parts (hi, lo)

@@ -9,8 +9,10 @@
 //   X(p, r): x transform of rows 8r..8r+7 of plane p (TMA row load; the Stockham stages
 //            exchange in the tile itself through XOR-swizzled slots), written to scratch
 //            slot p % R;
-//   Y(p, c): y transform of columns 8c..8c+7 of plane p (TMA box from the scratch slot;
-//            the tile is its own exchange buffer), written to the destination plane.
+//   Y(p, c): y transform of columns 8c..8c+7 of plane p (one contiguous bulk copy from the
+//            scratch slot, which holds a plane as N / 8 column tiles of 8 columns x N rows;
+//            the tile is its own exchange buffer), written to the destination plane. (At
+//            N = 512 the slot is row-major and the columns come as a TMA box.)
 // Order: X items of plane b and Y items of plane b - L, for b = 0, 1, ... (lag L planes).
 // Dependencies:
 //   Y(p, *) loads slot p % R only after all 32 X(p, *) items have stored (per-plane
@@ -159,6 +161,7 @@ struct XyL2Cfg;
 template <>
 struct XyL2Cfg<256> {
   static constexpr int C = 8, LAG = 40, RING = 72, TWN = 256;
+  static constexpr bool TILED = true;  // ring planes as column tiles (see k_xy_l2)
   using Plan = Radices<16, 16>;
   using Tw = TwRT256;
   // t[r*16 + k] = W_256^(r*k) = tw512[2*r*k] (r*k <= 225)
@@ -167,12 +170,9 @@ struct XyL2Cfg<256> {
   }
   static __device__ __forceinline__ SwzRow xslot(int c) { return SwzRow{c * 256}; }
   static __device__ __forceinline__ ColSwz8 yslot(int c) { return ColSwz8{c}; }
-  // C rows from the rows map / C columns of a scratch plane, one box each
+  // C rows from the rows map, one box
   static __device__ __forceinline__ void load_x(uint32_t d, const CUtensorMap *m, int row0, uint32_t bar) {
     tma_load_2d(d, m, 0, row0, bar);
-  }
-  static __device__ __forceinline__ void load_y(uint32_t d, const CUtensorMap *m, int x0, int slot, uint32_t bar) {
-    tma_load_3d(d, m, x0, 0, slot, bar);
   }
 };
 template <>
@@ -181,6 +181,7 @@ struct XyL2Cfg<128> {
   // 288 planes of 128 KiB (36 MiB), the same bytes as N = 256's. Lags of 96..192 planes
   // time the same within noise.
   static constexpr int C = 16, LAG = 160, RING = 288, TWN = 128;
+  static constexpr bool TILED = true;
   using Plan = Radices<16, 8>;
   using Tw = TwRT128;
   // t[j*16 + k] = W_128^(j*k) = tw512[4*j*k] (j < 8, k < 16)
@@ -192,9 +193,6 @@ struct XyL2Cfg<128> {
   static __device__ __forceinline__ void load_x(uint32_t d, const CUtensorMap *m, int row0, uint32_t bar) {
     tma_load_2d(d, m, 0, row0, bar);
   }
-  static __device__ __forceinline__ void load_y(uint32_t d, const CUtensorMap *m, int x0, int slot, uint32_t bar) {
-    tma_load_3d(d, m, x0, 0, slot, bar);
-  }
 };
 template <>
 struct XyL2Cfg<512> {
@@ -202,6 +200,9 @@ struct XyL2Cfg<512> {
   // planes of 2 MiB (36 MiB, as for the other sizes); lag / ring 8 / 16 and 14 / 24 time
   // no better.
   static constexpr int C = 4, LAG = 10, RING = 18, TWN = 768;
+  // Row-major ring planes: with 4-column tiles a warp's stores of one row would touch 8
+  // lines instead of 2 (measured 2% slower at 512^3).
+  static constexpr bool TILED = false;
   using Plan = Radices<16, 16, 2>;
   using Tw = TwRT512;
   static __device__ __forceinline__ float2 tw_entry(const float2 *tw512, int i) {
@@ -214,7 +215,8 @@ struct XyL2Cfg<512> {
   static __device__ __forceinline__ void load_x(uint32_t d, const CUtensorMap *m, int row0, uint32_t bar) {
     tma_load_3d(d, m, 0, 0, row0, bar);
   }
-  // a box is at most 256 long: rows 0..255 and 256..511 of the C columns
+  // C columns of a row-major ring plane; a box is at most 256 long: rows 0..255 and
+  // 256..511
   static __device__ __forceinline__ void load_y(uint32_t d, const CUtensorMap *m, int x0, int slot, uint32_t bar) {
     tma_load_3d(d, m, x0, 0, slot, bar);
     tma_load_3d(d + 256 * C * 8, m, x0, 256, slot, bar);
@@ -228,8 +230,8 @@ constexpr int xyl2_smem() {
   return 128 + XyL2Cfg<N>::C * N * 8 + XyL2Cfg<N>::TWN * 8 + 16;
 }
 
-// msrc: 2D map over the source rows (box {N, C}); mscr: 3D map over the Cfg::RING scratch
-// planes (box {C, N, 1}). ctr: 2 * np counters (X stores done, Y reads done) and the
+// msrc: 2D map over the source rows (box {N, C}); scratch: Cfg::RING planes of N x N;
+// mscr: 3D map over them (box {C, N, 1}), used where the ring planes are row-major. ctr: 2 * np counters (X stores done, Y reads done) and the
 // work counter at ctr[2 * np], all zero at launch.
 // TABLE: the planes belong to np / N cubes at unrelated addresses; plane p is plane p % N
 // of cube p / N, whose rows map is rmaps[p / N] (in device memory) and whose output base
@@ -279,7 +281,11 @@ __global__ void __launch_bounds__(kXyL2Threads, 8) k_xy_l2(const __grid_constant
         if (!wait_count(xdone + p, ITEMS, spin)) ok = false;
         asm volatile("fence.proxy.async.global;" ::: "memory");  // generic stores -> TMA reads
         mbar_arrive_expect_tx(bar, (uint32_t)(C * N * 8));
-        Cfg::load_y(smem_u32(tile), &mscr, tl * C, slot, bar);
+        if constexpr (Cfg::TILED)  // the column tile is one contiguous block
+          bulk_load(smem_u32(tile), scratch + (long long)slot * N * N + (long long)tl * N * C, (uint32_t)(C * N * 8),
+                    bar);
+        else
+          Cfg::load_y(smem_u32(tile), &mscr, tl * C, slot, bar);
       } else if constexpr (TABLE) {
         const unsigned long long q = (unsigned long long)p;
         const CUtensorMap *m = rmaps + q / N;
@@ -301,7 +307,7 @@ __global__ void __launch_bounds__(kXyL2Threads, 8) k_xy_l2(const __grid_constant
     float2 v[E];
     if (is_y) {
       const int c = threadIdx.x % C, t = threadIdx.x / C;
-      const ColSlot<C> lidx{c};  // the TMA box's layout
+      const ColSlot<C> lidx{c};  // the tile's layout: N rows of C values
 #pragma unroll
       for (int e = 0; e < E; ++e) v[e] = tile[lidx(t + e * T)];
       __syncthreads();
@@ -343,9 +349,19 @@ __global__ void __launch_bounds__(kXyL2Threads, 8) k_xy_l2(const __grid_constant
         if (threadIdx.x == 0 && !wait_count(yread + (p - RING), ITEMS, spin)) ok = false;
         __syncthreads();
       }
-      float2 *o = scratch + (long long)slot * N * N + (long long)(tl * C + c) * N + t;
+      if constexpr (Cfg::TILED) {
+        // column tile x / C of the slot holds its C columns of every row contiguously
+        float2 *o = scratch + (long long)slot * N * N + (tl * C + c) * C;
 #pragma unroll
-      for (int e = 0; e < E; ++e) o[e * T] = v[e];
+        for (int e = 0; e < E; ++e) {
+          const int x = t + e * T;
+          o[(x / C) * (N * C) + (x % C)] = v[e];
+        }
+      } else {
+        float2 *o = scratch + (long long)slot * N * N + (long long)(tl * C + c) * N + t;
+#pragma unroll
+        for (int e = 0; e < E; ++e) o[e * T] = v[e];
+      }
       __syncthreads();  // every thread's stores issued
       // The barrier orders every thread's stores before this release (cumulativity); a
       // thread of another warp than the one issuing the loads signals it.
