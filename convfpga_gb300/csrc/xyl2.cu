@@ -157,13 +157,12 @@ cudaError_t launch_xy_l2_tc(const float2 *src, float2 *dst, int nplanes, bool in
   using Cfg = XyL2Cfg<256>;
   if (nplanes <= 0) return cudaSuccess;
   if ((reinterpret_cast<uintptr_t>(dst) & 15u) != 0) return cudaErrorNotSupported;
-  CUtensorMap msrc, mscr;
+  CUtensorMap msrc;
   if (!encode_rows_map(&msrc, src, 256, (long long)nplanes * 256, Cfg::C)) return cudaErrorNotSupported;
   int ps, sms;
   Scratch *ring;
   cudaError_t e = xy_l2_setup<256>(nplanes, ps, sms, ring);
   if (e != cudaSuccess) return e;
-  if (!encode_cube_map(&mscr, ring->p, 256, Cfg::RING, 1, Cfg::C)) return cudaErrorNotSupported;
   static int done[2] = {0, 0};
   for (int i = 0; i < 2; ++i) {
     if (done[i]) continue;
@@ -192,7 +191,7 @@ cudaError_t launch_xy_l2_tc(const float2 *src, float2 *dst, int nplanes, bool in
   const long long items = 2LL * nplanes * (256 / Cfg::C);
   const unsigned grid = (unsigned)std::min<long long>(items, (long long)per_sm * sms);
   auto kern = inverse ? k_xy_l2_tc<true> : k_xy_l2_tc<false>;
-  kern<<<grid, kXyTcThreads, kXyTcSmem, s>>>(msrc, mscr, reinterpret_cast<float2 *>(ring->p), dst, nplanes, scale,
+  kern<<<grid, kXyTcThreads, kXyTcSmem, s>>>(msrc, reinterpret_cast<float2 *>(ring->p), dst, nplanes, scale,
                                              tw512, ctr, status, Cfg::LAG);
   return cudaGetLastError();
 }

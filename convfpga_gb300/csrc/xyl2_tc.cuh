@@ -6,7 +6,8 @@
 // Items (8 pencils each, one M = 128 tile per tensor-core stage):
 //   X(p, r): rows 8r..8r+7 of plane p (TMA box {256, 8}), row mapping of t5_fft256
 //            (thread m = 16 a + b: row a, positions b + 16 i), stored to scratch slot p % R;
-//   Y(p, c): columns 8c..8c+7 of the scratch slot (TMA box {8, 256, 1}), column mapping
+//   Y(p, c): columns 8c..8c+7 of the scratch slot (one 16 KB bulk copy of the slot's
+//            column tile c), column mapping
 //            (thread m = 8 a + b: column b, positions a + 16 i), stored to the output plane.
 // Dependencies, signals, item claiming and the no-deadlock argument are those of k_xy_l2.
 //
@@ -30,7 +31,7 @@ constexpr int kXyTcMinBlocks = 5;
 
 template <bool INV>
 __global__ void __launch_bounds__(kXyTcThreads, kXyTcMinBlocks)
-    k_xy_l2_tc(const __grid_constant__ CUtensorMap msrc, const __grid_constant__ CUtensorMap mscr, float2 *scratch,
+    k_xy_l2_tc(const __grid_constant__ CUtensorMap msrc, float2 *scratch,
                float2 *dst, long long np, float scale, const float2 *tw512, unsigned *ctr, unsigned *status,
                int lag_planes) {
   constexpr int N = 256, C = 8, ITEMS = N / C, TILE = N * C, RING = XyL2Cfg<256>::RING;
@@ -102,7 +103,8 @@ __global__ void __launch_bounds__(kXyTcThreads, kXyTcMinBlocks)
         if (!wait_count(xdone + p, ITEMS, spin)) ok = false;
         asm volatile("fence.proxy.async.global;" ::: "memory");  // generic stores -> TMA reads
         mbar_arrive_expect_tx(tbar, (uint32_t)(TILE * 8));
-        tma_load_3d(smem_u32(tile), &mscr, tl * C, 0, slot, tbar);
+        bulk_load(smem_u32(tile), scratch + (long long)slot * N * N + (long long)tl * N * C, (uint32_t)(TILE * 8),
+                  tbar);  // column tile tl of the slot: one contiguous block
       } else {
         mbar_arrive_expect_tx(tbar, (uint32_t)(TILE * 8));
         tma_load_2d(smem_u32(tile), &msrc, 0, (int)(p * N + tl * C), tbar);
@@ -148,9 +150,13 @@ __global__ void __launch_bounds__(kXyTcThreads, kXyTcMinBlocks)
         if (threadIdx.x == 0 && !wait_count(yread + (p - RING), ITEMS, spin)) ok = false;
         __syncthreads();
       }
-      float2 *o = scratch + (long long)slot * N * N + (long long)(tl * C + ia) * N + ib;
+      // the slot holds the plane as column tiles of C columns x N rows (as k_xy_l2)
+      float2 *o = scratch + (long long)slot * N * N + (tl * C + ia) * C;
 #pragma unroll
-      for (int k = 0; k < 16; ++k) o[16 * k] = v[k];
+      for (int k = 0; k < 16; ++k) {
+        const int x = ib + 16 * k;
+        o[(x / C) * (N * C) + (x % C)] = v[k];
+      }
       __syncthreads();  // every thread's stores issued
       if (threadIdx.x == 32) red_release_add_u32(xdone + p, 1u);
     }
