@@ -731,9 +731,10 @@ def run_configs(a) -> None:
     """The other single-GPU workloads, timed on device buffers (K steps after W warm-up
     steps, CUDA events): 64^3 x1 (signal and filter U[-1,1], normalised), 128^3 x8 (shared
     real periodic Gaussian filter, sigma 4) and 512^3 x1 (shared real periodic Gaussian
-    filter, sigma 6), the last on both the FP32 and the tensor-core split path. The real filters are passed as floats (CONVGPU_FILTER_REAL). Inputs
-    are generated on the device with the workloads' shapes; for timing, the 512^3 signal is
-    U[-1,1] noise instead of the workload's sum of Gaussian blobs."""
+    filter, sigma 6), the last on both the FP32 and the tensor-core split path. The real
+    filters are passed as floats (CONVGPU_FILTER_REAL). Inputs are generated on the device
+    with the workloads' shapes; for timing, the 512^3 signal is U[-1,1] noise instead of
+    the workload's sum of Gaussian blobs."""
     import torch
 
     import convfpga_gb300 as cg

@@ -42,9 +42,8 @@ constexpr int zconv_half_min_blocks() {
 }
 
 template <int N, int E, int COLS, class Plan>
-__global__ void __launch_bounds__(2 * COLS *(N / E), zconv_half_min_blocks<N>()) k_zconv_half(const __grid_constant__ CUtensorMap msig,
-                                                                 const __grid_constant__ CUtensorMap mhalf,
-                                                                 PassArgs a) {
+__global__ void __launch_bounds__(2 * COLS *(N / E), zconv_half_min_blocks<N>())
+    k_zconv_half(const __grid_constant__ CUtensorMap msig, const __grid_constant__ CUtensorMap mhalf, PassArgs a) {
   constexpr int T = N / E, TILE = N * COLS, FC = COLS + 2;
   constexpr int NBOX = N > 256 ? 256 : N, NLOADS = N / NBOX;
   constexpr int GROUPS = N / 2 / COLS;  // A tiles per row
@@ -77,7 +76,8 @@ __global__ void __launch_bounds__(2 * COLS *(N / E), zconv_half_min_blocks<N>())
     mbar_arrive_expect_tx(fbar, (uint32_t)(N * FC * 8));
     const int fz = (a.filt_vol_elems ? vol : 0) * N;
 #pragma unroll
-    for (int l = 0; l < NLOADS; ++l) tma_load_3d(smem_u32(ftile + l * NBOX * FC), &mhalf, x0, y, fz + l * NBOX, fbar);
+    for (int l = 0; l < NLOADS; ++l)
+      tma_load_3d(smem_u32(ftile + l * NBOX * FC), &mhalf, x0, y, fz + l * NBOX, fbar);
   }
   for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = a.tw512[i * (512 / N)];
   const int g = threadIdx.x / (COLS * T);  // 0: tile A, 1: tile B

@@ -231,8 +231,9 @@ constexpr int xyl2_smem() {
 }
 
 // msrc: 2D map over the source rows (box {N, C}); scratch: Cfg::RING planes of N x N;
-// mscr: 3D map over them (box {C, N, 1}), used where the ring planes are row-major. ctr: 2 * np counters (X stores done, Y reads done) and the
-// work counter at ctr[2 * np], all zero at launch.
+// mscr: 3D map over them (box {C, N, 1}), used where the ring planes are row-major.
+// ctr: 2 * np counters (X stores done, Y reads done) and the work counter at ctr[2 * np],
+// all zero at launch.
 // TABLE: the planes belong to np / N cubes at unrelated addresses; plane p is plane p % N
 // of cube p / N, whose rows map is rmaps[p / N] (in device memory) and whose output base
 // is dsts[p / N]; msrc and dst are unused (and rmaps, dsts otherwise).
