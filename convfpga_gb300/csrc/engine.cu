@@ -20,6 +20,7 @@
 // each run as one L2-staged launch. One cube of N <= 64 runs all of it in one cooperative
 // launch (persistent.cu: launch_small_conv).
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
 #include <atomic>
@@ -275,6 +276,19 @@ static int ensure_init_locked() {
 // (axis, op) slot with the pass's algorithmic bytes (one read + one write of every
 // cube, plus one read of the filter operand for the fused z pass).
 constexpr int kSlots = 14;  // slot = axis * 4 + op; 12 / 13: fused x+y forward / inverse
+static const char *const kSlotNames[kSlots] = {"x-fwd", "x-inv", "x-conv", "x-conv_fz", "y-fwd", "y-inv", "y-conv",
+                                               "y-conv_fz", "z-fwd", "z-inv", "z-conv", "z-conv_fz", "xy-fwd", "xy-inv"};
+
+// A named NVTX range on the calling thread around each pass's enqueue and each entry
+// point, so that Nsight Systems / Compute group the launches by pass; without a tool
+// attached each push / pop is a few nanoseconds.
+struct NvtxRange {
+  explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange &) = delete;
+  NvtxRange &operator=(const NvtxRange &) = delete;
+};
+
 struct PassRec {
   int slot;
   double bytes;
@@ -285,6 +299,7 @@ static std::vector<PassRec> g_prof_recs;
 
 static cudaError_t pass(int n, int axis, int op, const float2 *src, float2 *dst, const float2 *filt,
                         long long filt_vol, int nvol, float scale, cudaStream_t s, int tc) {
+  NvtxRange nv(kSlotNames[axis * 4 + op]);
   PassRec r{axis * 4 + op, 0.0, nullptr, nullptr};
   if (g_prof) {
     const double vol = (double)n * n * n * 8.0 * nvol;
@@ -315,6 +330,7 @@ static bool tc_kernels(int n, int tc) {
 // caller runs the x and y passes separately.
 static cudaError_t pass_xy(int n, const float2 *src, float2 *dst, int nvol, bool inverse, float scale,
                            cudaStream_t s, int tc = 0) {
+  NvtxRange nv(kSlotNames[12 + (inverse ? 1 : 0)]);
   PassRec r{12 + (inverse ? 1 : 0), 0.0, nullptr, nullptr};
   if (g_prof) {
     r.bytes = 4.0 * (double)n * n * n * 8.0 * nvol;  // the x and y passes it replaces
@@ -358,6 +374,7 @@ static bool use_xy(int n, int tc) {
 // x pass of real filter cubes (N^3 floats each) into complex spectra, profiled in the
 // x-fwd slot with its own bytes (4 read + 8 written per point).
 static cudaError_t pass_real(int n, const float *filt, float2 *spec, int count, cudaStream_t s) {
+  NvtxRange nv("x-fwd real");
   PassRec r{0 * 4 + OP_FWD, 0.0, nullptr, nullptr};
   if (g_prof) {
     r.bytes = 12.0 * (double)n * n * n * count;
@@ -384,6 +401,7 @@ static bool use_half(unsigned n, bool real, int tc) {
 // (C+2)/(2C) share of a full spectrum's bytes (C = 16 columns per tile below N = 256, 8 above).
 static cudaError_t pass_half(int n, int axis, int op, const void *src, float2 *dst, const float2 *filt,
                              long long filt_vol, int nvol, float scale, cudaStream_t s) {
+  NvtxRange nv(axis == 0 ? "x-fwd half" : (axis == 1 ? "y-fwd half" : (op == OP_CONV ? "z-conv half" : "z-fwd half")));
   PassRec r{axis * 4 + op, 0.0, nullptr, nullptr};
   if (g_prof) {
     const double v = (double)n * n * n, h = (double)n * n * half_spectrum_pitch(n);
@@ -590,6 +608,7 @@ int bridge_conv_device(unsigned n, const void *d_sig, const void *d_filt, void *
   std::lock_guard<std::recursive_mutex> lk(g.mu);
   int rc = ensure_init_locked();
   if (rc) return rc;
+  NvtxRange nv("convgpu_conv3d_device");
   cudaError_t e = g.ws.ensure(workspace_bytes_for(n, how_many, flags));
   if (e != cudaSuccess) return cuda_fail(e, "workspace");
   CallOrder order((cudaStream_t)stream);
@@ -608,6 +627,7 @@ int bridge_filter_spectrum_device(unsigned n, const void *d_filt, void *d_spec, 
   std::lock_guard<std::recursive_mutex> lk(g.mu);
   int rc = ensure_init_locked();
   if (rc) return rc;
+  NvtxRange nv("convgpu_filter_spectrum_device");
   CallOrder order((cudaStream_t)stream);
   cudaError_t e = enqueue_filter(n, (const float2 *)d_filt, (float2 *)d_spec, count, false, (cudaStream_t)stream);
   if (e != cudaSuccess) return cuda_fail(e, "launch");
@@ -672,6 +692,7 @@ int bridge_conv_uneven_device(const UnevenJob *jobs, unsigned njobs, const void 
   std::lock_guard<std::recursive_mutex> lk(g.mu);
   int rc = ensure_init_locked();
   if (rc) return rc;
+  NvtxRange nv("convgpu_conv3d_uneven_device");
   const bool normalize = (flags & kFlagNormalize) != 0;
   if (!(flags & (kFlagUnevenPerJob | kFlagTensorSplit | kFlagTensorBf16x3 | kFlagFilterIsSpectrum))) {
     std::string err;
@@ -912,6 +933,7 @@ Timing bridge_conv_host(unsigned n, const void *sig, const void *filt, void *out
   std::lock_guard<std::recursive_mutex> lk(g.mu);
   if (ensure_init_locked() != 0) return t;
   (void)mode;
+  NvtxRange nv("convgpu_conv3d_host");
   CallOrder order(g.sc);  // compute waits for device calls still in flight on other streams
 
   const bool per_signal = (flags & kFlagPerSignalFilter) != 0;
