@@ -66,6 +66,25 @@ def test_sizes_against_fp32_oracle(gpu, n, per_signal):
     assert rel_l2(ref64, out) < 1e-6
 
 
+@pytest.mark.parametrize("n", [16, 32])
+@pytest.mark.parametrize("flags", ["shared", "per_signal", "normalize"])
+def test_small_cubes_elementwise_against_fp64(gpu, n, flags):
+    """Every output value, not only the relative L2 norm: |out - ref| <= 1e-5 * max |ref| for
+    every element against the FP64 oracle (FP32 rounding of a 16- or 32-point transform
+    per axis is ~1e-7 relative to the largest value)."""
+    rng = np.random.default_rng(31 * n + len(flags))
+    b = 3
+    sig = _c64(rng, (b, n, n, n))
+    per_signal = flags == "per_signal"
+    filt = _c64(rng, (b, n, n, n) if per_signal else (n, n, n))
+    f = (gpu.FILTER_PER_SIGNAL if per_signal else 0) | (gpu.NORMALIZE if flags == "normalize" else 0)
+    out = dev_conv(gpu, sig, filt, f)
+    ref = conv3d(sig, filt, "fp64", normalize=flags == "normalize", engine="pocketfft")
+    err = np.abs(out.astype(np.complex128) - ref)
+    assert err.max() <= 1e-5 * np.abs(ref).max(), (err.max(), np.abs(ref).max())
+    assert gpu.device_status() == 0
+
+
 @pytest.mark.parametrize("n", [32, 256])
 @pytest.mark.parametrize("how_many", [1, 2, 3])
 def test_shared_filter_batches_against_fp32_oracle(gpu, full_spectra, n, how_many):
