@@ -125,3 +125,47 @@ def test_any_number_of_resident_ctas_completes(n, ncubes, ctas):
     order, items, ring = _schedule(n, ncubes)
     rng = random.Random(ctas * 7 + n)
     assert _simulate(order, items, ring, ctas, rng)
+
+
+def _tiled(n):
+    """TILED of XyL2Cfg<n> as written in the header."""
+    text = open(HEADER).read()
+    body = re.search(r"struct XyL2Cfg<%d>\s*\{(.*?)\n\};" % n, text, re.S).group(1)
+    return re.search(r"\bTILED\s*=\s*(true|false)", body).group(1) == "true"
+
+
+@pytest.mark.parametrize("n", [128, 256, 512])
+def test_ring_slot_layout(n):
+    """The X items' stores and the Y items' loads address the same slot positions: every
+    element of a plane is stored exactly once by the X items, and the Y item of column tile c
+    reads exactly columns C*c .. C*c+C-1 of every row, row by row in the order its threads
+    expect (position n of column j at n*C + j). Restates the index arithmetic of k_xy_l2: with
+    column tiles (N = 128, 256) an X thread (row y, lane t) stores x = t + e*T at
+    (x / C) * N * C + y * C + x % C and a Y item bulk-copies the N * C values from
+    c * N * C; with row-major slots (N = 512) the store is at y * N + x and the Y item's TMA
+    box lands row by row."""
+    import numpy as np
+
+    c_cols, _, _ = _cfg(n)
+    e_pts = 16
+    t_thr = n // e_pts
+    tiled = _tiled(n)
+    assert tiled == (n in (128, 256))
+    slot = np.full(n * n, -1, np.int64)
+    for tile in range(n // c_cols):            # X items of one plane
+        for c in range(c_cols):                # rows of the item
+            y = tile * c_cols + c
+            for t in range(t_thr):
+                for e in range(e_pts):
+                    x = t + e * t_thr
+                    addr = (x // c_cols) * n * c_cols + y * c_cols + x % c_cols if tiled else y * n + x
+                    assert slot[addr] == -1, "two stores to one slot position"
+                    slot[addr] = y * n + x     # which element lives there
+    assert (slot >= 0).all()
+    for tile in range(n // c_cols):            # Y items: what lands in shared memory
+        if tiled:
+            landed = slot[tile * n * c_cols:(tile + 1) * n * c_cols]
+        else:
+            landed = np.array([slot[r * n + tile * c_cols + j] for r in range(n) for j in range(c_cols)])
+        want = np.array([r * n + tile * c_cols + j for r in range(n) for j in range(c_cols)])
+        assert np.array_equal(landed, want)
